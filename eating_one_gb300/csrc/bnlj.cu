@@ -1,0 +1,275 @@
+// bnlj.cu - block nested-loop equi-join over all |R| x |S| pairs.
+//
+// Reference (joins/blockJoin_gpu/main_street): host tiles of PART = 2^18 per
+// side (nestLoopJoin.cc:326-519); per tile a `count` kernel and a `join`
+// kernel (join_gpu.cu:29-120) each stage 512 right tuples in shared memory and
+// compare them with one left tuple per thread, with a presum + DtoH of the
+// total in between - every compare runs twice.
+//
+// Here one kernel runs over all pairs once:
+//   - each CTA holds 4096 R vals in registers (16 per thread, coalesced load);
+//   - S is streamed through two 32 KB shared-memory buffers filled by 1-D TMA
+//     bulk copies (cp.async.bulk + mbarrier complete_tx), so the next S tile
+//     lands while the current one is compared;
+//   - the inner loop reads two S tuples per 16-byte broadcast load and tests
+//     each against the 16 registers with predicate-combined compares; only a
+//     hit leaves the loop;
+//   - matches are rare next to the 2^36 compares of the benchmark, so a hit
+//     takes its output slot from an atomic cursor (count-only mode sums
+//     per-thread counters instead).  Result order is not deterministic; the
+//     result multiset is.
+// Waits on the mbarrier are bounded by EJ_WAIT_LIMIT_NS and report
+// EJ_ERR_TIMEOUT instead of hanging.
+#include "ej_device.cuh"
+#include "ej_entry.h"
+
+namespace {
+
+constexpr int BN_THREADS = 256;
+constexpr int BN_RK = 16;                      // R vals per thread
+constexpr int BN_RCHUNK = BN_THREADS * BN_RK;  // R tuples per CTA
+constexpr int BN_STILE = 4096;                 // S tuples per shared-memory tile (32 KB)
+
+struct BnSmem {
+  int4 tile[2][BN_STILE / 2];  // two S tuples per int4
+  unsigned long long bar[2];
+  unsigned long long warp_tmp[BN_THREADS / 32 + 1];
+  int timed_out;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// bounded wait by one thread; true when the phase completed in time
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  const unsigned long long t0 = ej_globaltimer();
+  while (!mbar_try_wait(bar, parity)) {
+    if (ej_globaltimer() - t0 > EJ_WAIT_LIMIT_NS) return false;
+  }
+  return true;
+}
+
+template <bool USE_TMA>
+__device__ __forceinline__ void issue_tile(BnSmem& sm, int buf, const ej_tuple* S, uint64_t t0, uint32_t n) {
+  if (USE_TMA) {
+    if (threadIdx.x == 0) {
+      const uint32_t pairs = n >> 1;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&sm.bar[buf], pairs * 16u);
+      if (pairs) tma_load_1d(&sm.tile[buf][0], S + t0, pairs * 16u, &sm.bar[buf]);
+      if (n & 1u) {  // odd tail tuple: plain load (TMA sizes are multiples of 16 bytes)
+        const int2 last = *reinterpret_cast<const int2*>(S + t0 + n - 1);
+        reinterpret_cast<int2*>(&sm.tile[buf][0])[n - 1] = last;
+      }
+    }
+  } else {
+    int2* dst = reinterpret_cast<int2*>(&sm.tile[buf][0]);
+    const int2* src = reinterpret_cast<const int2*>(S + t0);
+    for (uint32_t i = threadIdx.x; i < n; i += BN_THREADS) dst[i] = __ldcs(src + i);
+  }
+}
+
+template <bool USE_TMA, bool COUNT_ONLY>
+__global__ void __launch_bounds__(BN_THREADS)
+bnl_kernel(const ej_tuple* __restrict__ R, uint64_t nR, const ej_tuple* __restrict__ S, uint64_t nS,
+           uint64_t s_per_cta, ej_result* __restrict__ out, uint64_t cap, unsigned long long* cursor,
+           ej_dev_status* st) {
+  extern __shared__ __align__(128) unsigned char bn_smem_raw[];
+  BnSmem& sm = *reinterpret_cast<BnSmem*>(bn_smem_raw);
+
+  // R chunk in registers; slots past nR repeat slot 0 and are masked on a hit
+  const uint64_t rbase = (uint64_t)blockIdx.x * BN_RCHUNK;
+  int r[BN_RK];
+  uint32_t valid = 0;
+#pragma unroll
+  for (int k = 0; k < BN_RK; k++) {
+    const uint64_t ri = rbase + (uint64_t)k * BN_THREADS + threadIdx.x;
+    if (ri < nR) {
+      r[k] = __ldg(&R[ri].val);
+      valid |= 1u << k;
+    }
+  }
+#pragma unroll
+  for (int k = 1; k < BN_RK; k++)
+    if (!(valid >> k & 1u)) r[k] = r[0];
+
+  const uint64_t s_begin = (uint64_t)blockIdx.y * s_per_cta;
+  const uint64_t s_end = min(nS, s_begin + s_per_cta);
+  const uint64_t ntiles = s_end > s_begin ? (s_end - s_begin + BN_STILE - 1) / BN_STILE : 0;
+
+  if (threadIdx.x == 0) {
+    sm.timed_out = 0;
+    if (USE_TMA) {
+      mbar_init(&sm.bar[0], 1);
+      mbar_init(&sm.bar[1], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+  }
+  __syncthreads();
+
+  unsigned long long local = 0;
+  if (ntiles) issue_tile<USE_TMA>(sm, 0, S, s_begin, (uint32_t)min((uint64_t)BN_STILE, s_end - s_begin));
+  uint64_t t;
+  for (t = 0; t < ntiles; t++) {
+    const int buf = (int)(t & 1);
+    const uint64_t t0 = s_begin + t * BN_STILE;
+    const uint32_t n = (uint32_t)min((uint64_t)BN_STILE, s_end - t0);
+    if (t + 1 < ntiles) {
+      const uint64_t t1 = t0 + BN_STILE;
+      issue_tile<USE_TMA>(sm, buf ^ 1, S, t1, (uint32_t)min((uint64_t)BN_STILE, s_end - t1));
+    }
+    if (USE_TMA) {
+      if (threadIdx.x == 0 && !mbar_wait_bounded(&sm.bar[buf], (unsigned)((t >> 1) & 1u))) sm.timed_out = 1;
+    }
+    __syncthreads();
+    if (sm.timed_out) break;
+    if (valid) {
+      const int4* tile = sm.tile[buf];
+      for (uint32_t k = 0; k < n; k += 2) {
+        const int4 q = tile[k >> 1];
+        bool h0 = false, h1 = false;
+#pragma unroll
+        for (int j = 0; j < BN_RK; j++) {
+          h0 |= (q.y == r[j]);
+          h1 |= (q.w == r[j]);
+        }
+        h1 = h1 && (k + 1 < n);
+        if (h0 | h1) {
+#pragma unroll 1
+          for (int half = 0; half < 2; half++) {
+            if (!(half ? h1 : h0)) continue;
+            const int skey = half ? q.z : q.x;
+            const int sval = half ? q.w : q.y;
+#pragma unroll
+            for (int j = 0; j < BN_RK; j++) {
+              if ((valid >> j & 1u) && r[j] == sval) {
+                if (COUNT_ONLY) {
+                  local++;
+                } else {
+                  const unsigned long long pos = atomicAdd(cursor, 1ull);
+                  if (pos < cap) {
+                    const uint64_t ri = rbase + (uint64_t)j * BN_THREADS + threadIdx.x;
+                    __stcs(reinterpret_cast<int4*>(out + pos), make_int4(__ldg(&R[ri].key), sval, skey, sval));
+                  }
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();  // everyone is done with `buf` before it is refilled
+  }
+  if (sm.timed_out && threadIdx.x == 0) {
+    ej_set_status(st, EJ_ERR_TIMEOUT, 2u);
+    // drain copies still in flight so none lands after the CTA exits
+    for (uint64_t u = t; u < ntiles && u <= t + 1; u++) mbar_wait_bounded(&sm.bar[u & 1], (unsigned)((u >> 1) & 1u));
+  }
+  if (COUNT_ONLY) {
+    unsigned long long total;
+    ej_block_exclusive_sum<BN_THREADS, unsigned long long>(local, sm.warp_tmp, &total);
+    if (threadIdx.x == 0 && total) atomicAdd(cursor, total);
+  }
+}
+
+template <bool USE_TMA, bool COUNT_ONLY>
+ej_status launch_bnl(ej_handle* h, dim3 grid, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                     uint64_t s_per_cta, ej_result* out, uint64_t cap) {
+  auto k = bnl_kernel<USE_TMA, COUNT_ONLY>;
+  EJ_CUDA(h, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BnSmem)));
+  k<<<grid, BN_THREADS, sizeof(BnSmem), h->stream>>>(R, nR, S, nS, s_per_cta, out, cap, h->d_words, h->d_status);
+  return ej_check_launch(h, "bnl_kernel");
+}
+
+}  // namespace
+
+static ej_status bnl_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                         ej_result* out, uint64_t cap, bool count_only) {
+  EJ_CUDA(h, cudaMemsetAsync(h->d_words, 0, sizeof(unsigned long long), h->stream));
+  if (nR == 0 || nS == 0) return EJ_OK;
+  const uint64_t rchunks = (nR + BN_RCHUNK - 1) / BN_RCHUNK;
+  if (rchunks > 0x7FFFFFFFull) return ej_fail(h, EJ_ERR_TOO_LARGE, "R too large for the nested loop");
+  // about four CTAs per SM in total; each S range is a whole number of tiles
+  const uint64_t want = (uint64_t)h->num_sms * 4;
+  uint64_t splits = (want + rchunks - 1) / rchunks;
+  const uint64_t stiles = (nS + BN_STILE - 1) / BN_STILE;
+  if (splits > stiles) splits = stiles;
+  if (splits > 65535) splits = 65535;
+  if (splits == 0) splits = 1;
+  const uint64_t tiles_per = (stiles + splits - 1) / splits;
+  const uint64_t s_per_cta = tiles_per * BN_STILE;
+  splits = (nS + s_per_cta - 1) / s_per_cta;
+  const dim3 grid((unsigned)rchunks, (unsigned)splits);
+  const bool tma = ((uintptr_t)S % 16) == 0;
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+  ej_status st;
+  if (count_only)
+    st = tma ? launch_bnl<true, true>(h, grid, R, nR, S, nS, s_per_cta, out, cap)
+             : launch_bnl<false, true>(h, grid, R, nR, S, nS, s_per_cta, out, cap);
+  else
+    st = tma ? launch_bnl<true, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap)
+             : launch_bnl<false, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap);
+  if (h->timing && st == EJ_OK) {
+    EJ_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
+    h->timed_pending = true;
+  }
+  return st;
+}
+
+extern "C" ej_status ej_bnl_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                                 ej_result* out, uint64_t out_cap, uint64_t* out_count) {
+  EJ_TRY(ej_begin(h));
+  EJ_TRY(ej_check_rel(h, "R", R, nR));
+  EJ_TRY(ej_check_rel(h, "S", S, nS));
+  EJ_TRY(ej_check_out(h, out, out_cap, out_count));
+  EJ_TRY(bnl_run(h, R, nR, S, nS, out, out_cap, false));
+  uint64_t count = 0;
+  EJ_TRY(ej_finish(h, &count));
+  *out_count = count;
+  return ej_capacity_result(h, count, out_cap);
+}
+
+extern "C" ej_status ej_bnl_join_count(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                                       uint64_t* out_count) {
+  EJ_TRY(ej_begin(h));
+  EJ_TRY(ej_check_rel(h, "R", R, nR));
+  EJ_TRY(ej_check_rel(h, "S", S, nS));
+  if (!out_count) return ej_fail(h, EJ_ERR_INVALID, "out_count is NULL");
+  EJ_TRY(bnl_run(h, R, nR, S, nS, nullptr, 0, true));
+  uint64_t count = 0;
+  EJ_TRY(ej_finish(h, &count));
+  *out_count = count;
+  return EJ_OK;
+}

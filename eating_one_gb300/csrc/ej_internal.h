@@ -1,0 +1,131 @@
+// ej_internal.h - host-side internals shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <string>
+
+#include "ej.h"
+
+// Device status word: the first error a kernel records wins (atomicCAS on code).
+struct ej_dev_status {
+  unsigned int code;  // ej_status
+  unsigned int info;  // kernel-specific detail (e.g. which wait gave up)
+  unsigned long long aux;
+};
+
+struct ej_zipf_cache {
+  double s = -1.0;
+  uint32_t domain = 0;
+  double* d_cdf = nullptr;
+};
+
+struct ej_handle {
+  int device = 0;
+  int num_sms = 0;
+  size_t l2_bytes = 0;
+  cudaStream_t stream = nullptr;
+  // scratch arena (bump allocation, reset per call)
+  void* arena = nullptr;
+  size_t arena_cap = 0;
+  size_t arena_peak = 0;
+  // small device words
+  ej_dev_status* d_status = nullptr;
+  unsigned long long* d_words = nullptr;  // [0] = join count, [1..7] scratch
+  unsigned long long* h_words = nullptr;  // pinned host mirror
+  ej_dev_status* h_status = nullptr;      // pinned host mirror of d_status
+  std::string last_error;
+  // phase timing
+  bool timing = false;
+  bool timed_pending = false;  // ev[0..3] recorded by the current call
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float phase_ms[3] = {0.f, 0.f, 0.f};
+  ej_zipf_cache zipf;
+  // tuning overrides (-1 / 0 = planner's choice)
+  int opt_partition_bits = -1;
+  int opt_bucket_delta = 0;
+  // host-buffer entry points: device staging owned separately from the arena
+  void* stage = nullptr;
+  size_t stage_cap = 0;
+};
+
+// Arena layout: callers first add every buffer to a plan, then reserve once.
+struct ej_plan_bytes {
+  size_t bytes = 0;
+  size_t add(size_t n) {
+    size_t off = bytes;
+    bytes += (n + 255) & ~size_t(255);
+    return off;
+  }
+};
+
+ej_status ej_fail(ej_handle* h, ej_status s, const char* fmt, ...);
+ej_status ej_arena_reserve(ej_handle* h, size_t bytes);
+inline char* ej_arena_at(ej_handle* h, size_t off) { return static_cast<char*>(h->arena) + off; }
+ej_status ej_check_launch(ej_handle* h, const char* what);
+ej_status ej_read_count(ej_handle* h, uint64_t* out_count);  // sync + read d_words[0]
+ej_status ej_take_status(ej_handle* h);                      // sync + read/clear d_status
+
+#define EJ_CUDA(h, call)                                                                  \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return ej_fail((h), EJ_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),  \
+                     __FILE__, __LINE__);                                                 \
+  } while (0)
+
+#define EJ_TRY(...)                  \
+  do {                               \
+    ej_status s_ = (__VA_ARGS__);    \
+    if (s_ != EJ_OK) return s_;      \
+  } while (0)
+
+static inline uint32_t ej_ceil_log2(uint64_t x) {
+  uint32_t b = 0;
+  while ((uint64_t(1) << b) < x) b++;
+  return b;
+}
+
+// ---- prefix scan (scan.cu) ----------------------------------------------
+// Exclusive scan of n inputs into n+1 outputs (out[n] = total).  `scratch`
+// must hold ej_scan_scratch_bytes(n) bytes of device memory.
+size_t ej_scan_scratch_bytes(uint64_t n);
+ej_status ej_scan_u32_u32(ej_handle* h, const uint32_t* in, uint64_t n, uint32_t* out, void* scratch);
+ej_status ej_scan_u32_u64(ej_handle* h, const uint32_t* in, uint64_t n, unsigned long long* out,
+                          void* scratch);
+ej_status ej_scan_u64_u64(ej_handle* h, const unsigned long long* in, uint64_t n,
+                          unsigned long long* out, void* scratch);
+
+// ---- radix partitioning (radix.cu) ---------------------------------------
+// Stable partition of tuples by digit = (key(val) >> shift) & ((1<<bits)-1),
+// key = hash32(val) (EJ_DIGIT_HASH) or the order-preserving unsigned image of
+// the signed val (EJ_DIGIT_VALUE, for sorting).
+enum { EJ_DIGIT_HASH = 0, EJ_DIGIT_VALUE = 1 };
+struct ej_radix_plan {
+  uint64_t n = 0;
+  uint32_t ntiles = 0;
+  size_t hist_off = 0, offs_off = 0, scan_off = 0;  // arena offsets
+};
+uint32_t ej_radix_tiles(uint64_t n);
+void ej_radix_plan_add(ej_plan_bytes& p, ej_radix_plan& rp, uint64_t n);
+ej_status ej_radix_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
+                        uint32_t shift, uint32_t bits, int digit_kind = EJ_DIGIT_HASH);
+
+// ---- probe targets (hash_join.cu) -----------------------------------------
+// EJ_TABLE_HASH: R sorted by bucket id (top `hb` bits of hash32(val)) plus
+//   bucket starts; a probe scans its bucket and compares val.
+// EJ_TABLE_SORTED: R sorted by val; a probe binary-searches the matching run,
+//   narrowed first by a fence of every 256th val.
+enum { EJ_TABLE_HASH = 0, EJ_TABLE_SORTED = 1 };
+constexpr uint32_t EJ_FENCE_STRIDE = 256;
+struct ej_table_view {
+  int kind = EJ_TABLE_HASH;
+  const ej_tuple* rs = nullptr;      // R in bucket (or val) order
+  const uint32_t* start = nullptr;   // [2^hb + 1] (hash)
+  const int32_t* fence = nullptr;    // [nfence] (sorted)
+  uint64_t nR = 0;
+  uint32_t hb = 1;
+  uint32_t nfence = 0;
+};
+uint32_t ej_table_bucket_bits(uint64_t nR, int delta = 0);

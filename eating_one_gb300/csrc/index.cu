@@ -1,0 +1,311 @@
+// index.cu - device-resident hash and sort indexes, index joins, the left
+// outer join and the 3-way star join.
+//
+// The reference builds both indexes on the CPU and uploads them (hash index:
+// joins/innerJoin_gpu/main_street/inner-idx-bnlj.cc:148-181, `val % 2^24`
+// buckets; sort index: joins/innerJoin_gpu/sort_index/main_street/
+// inner-idx-bnlj.cc:175-217, recursive quicksort of BUCKET{val,adr}), then
+// probes one S tuple per thread (count.cu:16-48 / join_gpu.cu:8-86;
+// sort_index join_gpu.cu:10-113).  Here both indexes are built on the device
+// with the LSD radix passes of radix.cu: the hash index is the bucketised
+// table of hash_join.cu, the sort index is R sorted stably by val plus a fence
+// of every 256th val that narrows the binary search to one 2 KB segment.
+#include "ej_device.cuh"
+#include "ej_entry.h"
+#include "hash_join.cuh"
+
+struct ej_index {
+  int kind = EJ_TABLE_HASH;
+  int device = 0;
+  uint64_t nR = 0;
+  ej_tuple* rs = nullptr;  // device, owned
+  void* aux = nullptr;     // device, owned: bucket starts or fence
+  ej_table_view view;
+};
+
+// ---- index lifecycle ------------------------------------------------------
+
+static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t nR, ej_index** out) {
+  EJ_TRY(ej_begin(h));
+  EJ_TRY(ej_check_rel(h, "R", R, nR));
+  if (!out) return ej_fail(h, EJ_ERR_INVALID, "index out-pointer is NULL");
+  *out = nullptr;
+  ej_plan_bytes p;
+  ej_table_plan_t tp;
+  ej_table_plan(p, tp, nR, /*own_storage=*/true, kind, h->opt_bucket_delta);
+  EJ_TRY(ej_arena_reserve(h, p.bytes));
+  ej_index* ix = new ej_index();
+  ix->kind = kind;
+  ix->device = h->device;
+  ix->nR = nR;
+  const size_t rs_bytes = (size_t)(nR ? nR : 1) * sizeof(ej_tuple);
+  const size_t aux_bytes = kind == EJ_TABLE_HASH ? ((size_t(1) << tp.hb) + 1) * sizeof(uint32_t)
+                                                 : (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
+  if (cudaMalloc(&ix->rs, rs_bytes) != cudaSuccess || cudaMalloc(&ix->aux, aux_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(ix->rs);
+    cudaFree(ix->aux);
+    delete ix;
+    return ej_fail(h, EJ_ERR_NOMEM, "index storage of %zu bytes could not be allocated", rs_bytes + aux_bytes);
+  }
+  ej_status st = ej_table_build(h, tp, R, ix->rs, ix->aux, &ix->view);
+  if (st == EJ_OK) st = ej_finish(h, nullptr);
+  if (st != EJ_OK) {
+    cudaFree(ix->rs);
+    cudaFree(ix->aux);
+    delete ix;
+    return st;
+  }
+  *out = ix;
+  return EJ_OK;
+}
+
+extern "C" ej_status ej_hash_index_build(ej_handle* h, const ej_tuple* R, uint64_t nR, ej_index** out) {
+  return index_build(h, EJ_TABLE_HASH, R, nR, out);
+}
+
+extern "C" ej_status ej_sort_index_build(ej_handle* h, const ej_tuple* R, uint64_t nR, ej_index** out) {
+  return index_build(h, EJ_TABLE_SORTED, R, nR, out);
+}
+
+extern "C" ej_status ej_index_free(ej_handle* h, ej_index* idx) {
+  if (!h || !idx) return EJ_ERR_INVALID;
+  EJ_CUDA(h, cudaSetDevice(idx->device));
+  EJ_CUDA(h, cudaStreamSynchronize(h->stream));
+  cudaFree(idx->rs);
+  cudaFree(idx->aux);
+  delete idx;
+  return EJ_OK;
+}
+
+// ---- index probes ------------------------------------------------------------
+
+static ej_status index_probe(ej_handle* h, const ej_index* ix, const ej_tuple* S, uint64_t nS, bool outer,
+                             bool count_only, ej_result* out, uint64_t cap, uint64_t* out_count) {
+  EJ_TRY(ej_begin(h));
+  if (!ix) return ej_fail(h, EJ_ERR_INVALID, "index is NULL");
+  if (ix->device != h->device) return ej_fail(h, EJ_ERR_INVALID, "index lives on another device");
+  EJ_TRY(ej_check_rel(h, "S", S, nS));
+  if (count_only) {
+    if (!out_count) return ej_fail(h, EJ_ERR_INVALID, "out_count is NULL");
+  } else {
+    EJ_TRY(ej_check_out(h, out, cap, out_count));
+  }
+  // hash index: partition S by hash when the index outgrows L2; a sorted
+  // index is probed in place (its fence keeps the search top in L2)
+  const uint32_t pb = ix->kind == EJ_TABLE_HASH ? ej_probe_partition_bits(h, ix->nR, nS) : 0u;
+  ej_plan_bytes p;
+  ej_probe_layout L;
+  ej_probe_layout_add(p, L, nS, pb);
+  EJ_TRY(ej_arena_reserve(h, p.bytes));
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  EJ_TRY(ej_probe_exec(h, L, ix->view, S, outer, count_only, out, cap, h->d_words));
+  uint64_t count = 0;
+  EJ_TRY(ej_finish(h, &count));
+  *out_count = count;
+  return count_only ? EJ_OK : ej_capacity_result(h, count, cap);
+}
+
+extern "C" ej_status ej_index_join(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS,
+                                   ej_result* out, uint64_t out_cap, uint64_t* out_count) {
+  return index_probe(h, idx, S, nS, false, false, out, out_cap, out_count);
+}
+
+extern "C" ej_status ej_index_join_count(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS,
+                                         uint64_t* out_count) {
+  return index_probe(h, idx, S, nS, false, true, nullptr, 0, out_count);
+}
+
+extern "C" ej_status ej_index_left_outer_join(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS,
+                                              ej_result* out, uint64_t out_cap, uint64_t* out_count) {
+  return index_probe(h, idx, S, nS, true, false, out, out_cap, out_count);
+}
+
+static ej_status build_and_probe(ej_handle* h, int kind, bool outer, const ej_tuple* R, uint64_t nR,
+                                 const ej_tuple* S, uint64_t nS, ej_result* out, uint64_t out_cap,
+                                 uint64_t* out_count) {
+  ej_index* ix = nullptr;
+  EJ_TRY(index_build(h, kind, R, nR, &ix));
+  const ej_status st = index_probe(h, ix, S, nS, outer, false, out, out_cap, out_count);
+  const std::string err = h->last_error;
+  ej_index_free(h, ix);
+  h->last_error = err;
+  return st;
+}
+
+extern "C" ej_status ej_hash_index_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                                        uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count) {
+  return build_and_probe(h, EJ_TABLE_HASH, false, R, nR, S, nS, out, out_cap, out_count);
+}
+
+extern "C" ej_status ej_sort_index_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                                        uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count) {
+  return build_and_probe(h, EJ_TABLE_SORTED, false, R, nR, S, nS, out, out_cap, out_count);
+}
+
+// Left outer join on a transient hash table held in the arena.
+extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                                        uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count) {
+  EJ_TRY(ej_begin(h));
+  EJ_TRY(ej_check_rel(h, "R", R, nR));
+  EJ_TRY(ej_check_rel(h, "S", S, nS));
+  EJ_TRY(ej_check_out(h, out, out_cap, out_count));
+  const uint32_t pb = ej_probe_partition_bits(h, nR, nS);
+  ej_plan_bytes p;
+  ej_table_plan_t tp;
+  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, h->opt_bucket_delta);
+  ej_probe_layout L;
+  ej_probe_layout_add(p, L, nS, pb);
+  EJ_TRY(ej_arena_reserve(h, p.bytes));
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  ej_table_view t;
+  EJ_TRY(ej_table_build(h, tp, R, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.rs_off)),
+                        ej_arena_at(h, tp.start_off), &t));
+  EJ_TRY(ej_probe_exec(h, L, t, S, /*outer=*/true, false, out, out_cap, h->d_words));
+  uint64_t count = 0;
+  EJ_TRY(ej_finish(h, &count));
+  *out_count = count;
+  return ej_capacity_result(h, count, out_cap);
+}
+
+// ---- 3-way star join ------------------------------------------------------------
+
+namespace {
+
+constexpr int ST_THREADS = 256;
+constexpr int ST_ITEMS = 4;
+constexpr int ST_TILE = ST_THREADS * ST_ITEMS;
+
+__device__ __forceinline__ void bucket_range(const ej_table_view& t, int32_t v, uint32_t& lo, uint32_t& hi) {
+  const uint32_t b = ej_hash32((uint32_t)v) >> (32u - t.hb);
+  lo = __ldg(t.start + b);
+  hi = __ldg(t.start + b + 1);
+}
+
+__device__ __forceinline__ uint32_t bucket_matches(const ej_table_view& t, uint32_t lo, uint32_t hi, int32_t v) {
+  const int* rv = reinterpret_cast<const int*>(t.rs) + 1;
+  uint32_t m = 0;
+  for (uint32_t i = lo; i < hi; i++) m += (__ldg(rv + 2 * (uint64_t)i) == v);
+  return m;
+}
+
+__global__ void __launch_bounds__(ST_THREADS)
+star_count_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ F2, uint64_t nF, ej_table_view t1,
+                  ej_table_view t2, unsigned long long* __restrict__ tile_count) {
+  __shared__ unsigned long long warp_tmp[ST_THREADS / 32 + 1];
+  const uint64_t base = (uint64_t)blockIdx.x * ST_TILE;
+  unsigned long long c = 0;
+#pragma unroll
+  for (int j = 0; j < ST_ITEMS; j++) {
+    const uint64_t idx = base + (uint64_t)j * ST_THREADS + threadIdx.x;
+    if (idx >= nF) continue;
+    const int32_t v1 = __ldcs(&F1[idx].val), v2 = __ldcs(&F2[idx].val);
+    uint32_t lo1, hi1, lo2, hi2;
+    bucket_range(t1, v1, lo1, hi1);
+    bucket_range(t2, v2, lo2, hi2);
+    const uint32_t m1 = bucket_matches(t1, lo1, hi1, v1);
+    const uint32_t m2 = m1 ? bucket_matches(t2, lo2, hi2, v2) : 0u;
+    c += (unsigned long long)m1 * m2;
+  }
+  unsigned long long total;
+  ej_block_exclusive_sum<ST_THREADS, unsigned long long>(c, warp_tmp, &total);
+  if (threadIdx.x == 0) tile_count[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(ST_THREADS)
+star_write_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ F2, uint64_t nF, ej_table_view t1,
+                  ej_table_view t2, const unsigned long long* __restrict__ tile_off, uint64_t ntiles,
+                  ej_star_result* __restrict__ out, uint64_t cap, ej_dev_status* st) {
+  __shared__ unsigned long long warp_tmp[ST_THREADS / 32 + 1];
+  const uint64_t base = (uint64_t)blockIdx.x * ST_TILE;
+  int2 f1[ST_ITEMS], f2[ST_ITEMS];
+  uint32_t lo1[ST_ITEMS], hi1[ST_ITEMS], lo2[ST_ITEMS], hi2[ST_ITEMS];
+  unsigned long long c = 0;
+#pragma unroll
+  for (int j = 0; j < ST_ITEMS; j++) {
+    const uint64_t idx = base + (uint64_t)j * ST_THREADS + threadIdx.x;
+    lo1[j] = hi1[j] = lo2[j] = hi2[j] = 0;
+    if (idx >= nF) continue;
+    f1[j] = __ldcs(reinterpret_cast<const int2*>(F1) + idx);
+    f2[j] = __ldcs(reinterpret_cast<const int2*>(F2) + idx);
+    bucket_range(t1, f1[j].y, lo1[j], hi1[j]);
+    bucket_range(t2, f2[j].y, lo2[j], hi2[j]);
+    const uint32_t m1 = bucket_matches(t1, lo1[j], hi1[j], f1[j].y);
+    const uint32_t m2 = m1 ? bucket_matches(t2, lo2[j], hi2[j], f2[j].y) : 0u;
+    if (m2 == 0) hi1[j] = lo1[j];  // nothing to write for this fact row
+    c += (unsigned long long)m1 * m2;
+  }
+  unsigned long long total;
+  unsigned long long pos = ej_block_exclusive_sum<ST_THREADS, unsigned long long>(c, warp_tmp, &total);
+  pos += tile_off[blockIdx.x];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && tile_off[ntiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+#pragma unroll
+  for (int j = 0; j < ST_ITEMS; j++) {
+    for (uint32_t a = lo1[j]; a < hi1[j]; a++) {
+      const int2 d1 = __ldg(reinterpret_cast<const int2*>(t1.rs) + a);
+      if (d1.y != f1[j].y) continue;
+      for (uint32_t b = lo2[j]; b < hi2[j]; b++) {
+        const int2 d2 = __ldg(reinterpret_cast<const int2*>(t2.rs) + b);
+        if (d2.y != f2[j].y) continue;
+        if (pos < cap) {
+          int4* o = reinterpret_cast<int4*>(out + pos);
+          __stcs(o, make_int4(d1.x, d1.y, f1[j].x, f1[j].y));
+          __stcs(o + 1, make_int4(d2.x, d2.y, f2[j].x, f2[j].y));
+        }
+        pos++;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tuple* F2, uint64_t nF,
+                                   const ej_tuple* D1, uint64_t nD1, const ej_tuple* D2, uint64_t nD2,
+                                   ej_star_result* out, uint64_t out_cap, uint64_t* out_count) {
+  EJ_TRY(ej_begin(h));
+  EJ_TRY(ej_check_rel(h, "F1", F1, nF));
+  EJ_TRY(ej_check_rel(h, "F2", F2, nF));
+  EJ_TRY(ej_check_rel(h, "D1", D1, nD1));
+  EJ_TRY(ej_check_rel(h, "D2", D2, nD2));
+  EJ_TRY(ej_check_out(h, out, out_cap, out_count));
+  ej_plan_bytes p;
+  ej_table_plan_t tp1, tp2;
+  ej_table_plan(p, tp1, nD1, false, EJ_TABLE_HASH);
+  ej_table_plan(p, tp2, nD2, false, EJ_TABLE_HASH);
+  const uint64_t ntiles = (nF + ST_TILE - 1) / ST_TILE;
+  const size_t count_off = p.add((ntiles + 1) * sizeof(unsigned long long));
+  const size_t off_off = p.add((ntiles + 1) * sizeof(unsigned long long));
+  const size_t scan_off = p.add(ej_scan_scratch_bytes(ntiles));
+  EJ_TRY(ej_arena_reserve(h, p.bytes));
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  ej_table_view t1, t2;
+  EJ_TRY(ej_table_build(h, tp1, D1, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp1.rs_off)),
+                        ej_arena_at(h, tp1.start_off), &t1));
+  EJ_TRY(ej_table_build(h, tp2, D2, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp2.rs_off)),
+                        ej_arena_at(h, tp2.start_off), &t2));
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+  unsigned long long* tcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, count_off));
+  unsigned long long* toff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, off_off));
+  if (ntiles) {
+    star_count_kernel<<<(unsigned)ntiles, ST_THREADS, 0, h->stream>>>(F1, F2, nF, t1, t2, tcount);
+    EJ_TRY(ej_check_launch(h, "star_count_kernel"));
+  }
+  EJ_TRY(ej_scan_u64_u64(h, tcount, ntiles, toff, ej_arena_at(h, scan_off)));
+  EJ_CUDA(h, cudaMemcpyAsync(h->d_words, toff + ntiles, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                             h->stream));
+  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+  if (ntiles) {
+    star_write_kernel<<<(unsigned)ntiles, ST_THREADS, 0, h->stream>>>(F1, F2, nF, t1, t2, toff, ntiles, out, out_cap,
+                                                                     h->d_status);
+    EJ_TRY(ej_check_launch(h, "star_write_kernel"));
+  }
+  if (h->timing) {
+    EJ_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
+    h->timed_pending = true;
+  }
+  uint64_t count = 0;
+  EJ_TRY(ej_finish(h, &count));
+  *out_count = count;
+  return ej_capacity_result(h, count, out_cap);
+}

@@ -1,0 +1,193 @@
+// radix.cu - stable radix partitioning of TUPLE arrays by hash digits.
+//
+// Replaces the reference's radix partitioner (joins/hashJoin_gpu/main_street/
+// partitioning.cu:15-271 lcount/rcount_partitioning + lpartitioning/
+// rpartitioning, driven by hj.cc:430-534 and :702-829): 16-thread blocks that
+// each walk 256 consecutive tuples, one 6-bit digit per pass, a host
+// round-trip per pass.  Here one pass is three launches on the stream:
+//   1. rx_hist_kernel    per 8192-tuple tile, digit counts in shared memory
+//                        (warp-aggregated with __match_any_sync, so skewed
+//                        digits do not serialise on atomics), stored
+//                        digit-major: hist[digit * ntiles + tile];
+//   2. look-back scan    of the digit-major histogram gives every (digit, tile)
+//                        its global output offset (scan.cu);
+//   3. rx_scatter_kernel stages the tile in shared memory, ranks it stably by
+//                        digit (warp-ordered match_any ranking), and writes it
+//                        digit run by digit run, so consecutive threads store
+//                        consecutive addresses.
+// Digits are up to 8 bits of hash32(val).  Positions are 32-bit: n < 2^32.
+#include "ej_device.cuh"
+
+namespace {
+
+constexpr int RX_THREADS = 256;
+constexpr int RX_WARPS = RX_THREADS / 32;
+constexpr int RX_TILE = 8192;
+constexpr int RX_WARP_SPAN = RX_TILE / RX_WARPS;  // 1024 consecutive tuples per warp
+constexpr int RX_ROUNDS = RX_WARP_SPAN / 32;      // 32
+constexpr int RX_MAX_DIGITS = 256;
+
+template <int KIND>
+__device__ __forceinline__ uint32_t rx_digit(int32_t val, uint32_t shift, uint32_t mask) {
+  const uint32_t key = KIND == EJ_DIGIT_HASH ? ej_hash32((uint32_t)val) : ((uint32_t)val ^ 0x80000000u);
+  return (key >> shift) & mask;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(RX_THREADS)
+rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, uint32_t* __restrict__ hist, uint32_t ntiles,
+               uint32_t shift, uint32_t mask) {
+  __shared__ uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];
+  const uint32_t ndig = mask + 1u;
+  for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&cnt[0][0])[i] = 0u;
+  __syncthreads();
+  const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint64_t wbase = (uint64_t)blockIdx.x * RX_TILE + (uint64_t)warp * RX_WARP_SPAN;
+  const int* vals = reinterpret_cast<const int*>(in) + 1;  // .val of tuple i at vals[2*i]
+  int v[RX_ROUNDS];
+#pragma unroll
+  for (int r = 0; r < RX_ROUNDS; r++) {
+    const uint64_t idx = wbase + (uint64_t)r * 32u + lane;
+    v[r] = idx < n ? __ldcs(vals + 2 * idx) : 0;
+  }
+#pragma unroll
+  for (int r = 0; r < RX_ROUNDS; r++) {
+    const uint64_t idx = wbase + (uint64_t)r * 32u + lane;
+    const bool valid = idx < n;
+    const uint32_t d = valid ? rx_digit<KIND>(v[r], shift, mask) : 0xFFFFFFFFu;
+    const unsigned int peers = __match_any_sync(EJ_FULL_MASK, d);
+    if (valid && lane == (unsigned)(__ffs(peers) - 1)) cnt[warp][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  for (uint32_t d = threadIdx.x; d < ndig; d += RX_THREADS) {
+    uint32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < RX_WARPS; w++) t += cnt[w][d];
+    hist[(uint64_t)d * ntiles + blockIdx.x] = t;
+  }
+}
+
+struct RxScatterSmem {
+  ej_tuple tile[RX_TILE];              // 64 KB
+  uint16_t perm[RX_TILE];              // 16 KB: sorted position -> tile index
+  uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];  // 8 KB
+  uint32_t digit_start[RX_MAX_DIGITS];
+  uint32_t gbase[RX_MAX_DIGITS];
+  uint32_t warp_tmp[RX_WARPS + 1];
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(RX_THREADS)
+rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, ej_tuple* __restrict__ out,
+                  const uint32_t* __restrict__ offs, uint32_t ntiles, uint32_t shift, uint32_t mask) {
+  extern __shared__ __align__(16) unsigned char rx_smem_raw[];
+  RxScatterSmem& sm = *reinterpret_cast<RxScatterSmem*>(rx_smem_raw);
+  const uint32_t ndig = mask + 1u;
+  const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint64_t tbase = (uint64_t)blockIdx.x * RX_TILE;
+  const uint32_t tile_n = (uint32_t)min((uint64_t)RX_TILE, n - tbase);
+
+  // 1. stage the tile (coalesced 8-byte loads, streaming: read once)
+  const uint2* src = reinterpret_cast<const uint2*>(in + tbase);
+  uint2* dst = reinterpret_cast<uint2*>(sm.tile);
+#pragma unroll 8
+  for (uint32_t i = threadIdx.x; i < tile_n; i += RX_THREADS) dst[i] = __ldcs(src + i);
+  for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&sm.cnt[0][0])[i] = 0u;
+  __syncthreads();
+
+  // 2. per-warp digit counts over the warp's consecutive span
+  const uint32_t wbase = warp * RX_WARP_SPAN;
+  for (int r = 0; r < RX_ROUNDS; r++) {
+    const uint32_t i = wbase + r * 32u + lane;
+    const bool valid = i < tile_n;
+    const uint32_t d = valid ? rx_digit<KIND>(sm.tile[i].val, shift, mask) : 0xFFFFFFFFu;
+    const unsigned int peers = __match_any_sync(EJ_FULL_MASK, d);
+    if (valid && lane == (unsigned)(__ffs(peers) - 1)) sm.cnt[warp][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // 3. warp offsets within each digit, digit starts within the tile, global bases
+  uint32_t total = 0;
+  if (threadIdx.x < ndig) {
+    const uint32_t d = threadIdx.x;
+#pragma unroll
+    for (int w = 0; w < RX_WARPS; w++) {
+      const uint32_t c = sm.cnt[w][d];
+      sm.cnt[w][d] = total;
+      total += c;
+    }
+  }
+  uint32_t all;
+  const uint32_t dstart = ej_block_exclusive_sum<RX_THREADS, uint32_t>(total, sm.warp_tmp, &all);
+  if (threadIdx.x < ndig) {
+    sm.digit_start[threadIdx.x] = dstart;
+    sm.gbase[threadIdx.x] = offs[(uint64_t)threadIdx.x * ntiles + blockIdx.x] - dstart;
+  }
+  __syncthreads();
+
+  // 4. stable rank: warp order, then round order, then lane order
+  for (int r = 0; r < RX_ROUNDS; r++) {
+    const uint32_t i = wbase + r * 32u + lane;
+    const bool valid = i < tile_n;
+    const uint32_t d = valid ? rx_digit<KIND>(sm.tile[i].val, shift, mask) : 0xFFFFFFFFu;
+    const unsigned int peers = __match_any_sync(EJ_FULL_MASK, d);
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (valid && (int)lane == leader) {
+      old = sm.cnt[warp][d];
+      sm.cnt[warp][d] = old + __popc(peers);
+    }
+    old = __shfl_sync(EJ_FULL_MASK, old, leader);
+    if (valid) sm.perm[sm.digit_start[d] + old + __popc(peers & ej_lanemask_lt())] = (uint16_t)i;
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // 5. write digit runs: sorted position k goes to gbase[digit] + k
+  for (uint32_t k = threadIdx.x; k < tile_n; k += RX_THREADS) {
+    const ej_tuple t = sm.tile[sm.perm[k]];
+    const uint32_t d = rx_digit<KIND>(t.val, shift, mask);
+    reinterpret_cast<uint2*>(out)[sm.gbase[d] + k] = make_uint2((uint32_t)t.key, (uint32_t)t.val);
+  }
+}
+
+}  // namespace
+
+uint32_t ej_radix_tiles(uint64_t n) { return (uint32_t)((n + RX_TILE - 1) / RX_TILE); }
+
+void ej_radix_plan_add(ej_plan_bytes& p, ej_radix_plan& rp, uint64_t n) {
+  rp.n = n;
+  rp.ntiles = ej_radix_tiles(n);
+  const uint64_t cells = (uint64_t)rp.ntiles * RX_MAX_DIGITS;
+  rp.hist_off = p.add(cells * sizeof(uint32_t));
+  rp.offs_off = p.add((cells + 1) * sizeof(uint32_t));
+  rp.scan_off = p.add(ej_scan_scratch_bytes(cells));
+}
+
+template <int KIND>
+static ej_status radix_pass_kind(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
+                                 uint32_t shift, uint32_t bits) {
+  const uint32_t mask = (1u << bits) - 1u;
+  const uint64_t cells = (uint64_t)rp.ntiles << bits;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(ej_arena_at(h, rp.hist_off));
+  uint32_t* offs = reinterpret_cast<uint32_t*>(ej_arena_at(h, rp.offs_off));
+  rx_hist_kernel<KIND><<<rp.ntiles, RX_THREADS, 0, h->stream>>>(in, rp.n, hist, rp.ntiles, shift, mask);
+  EJ_TRY(ej_check_launch(h, "rx_hist_kernel"));
+  EJ_TRY(ej_scan_u32_u32(h, hist, cells, offs, ej_arena_at(h, rp.scan_off)));
+  EJ_CUDA(h, cudaFuncSetAttribute(rx_scatter_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(RxScatterSmem)));
+  rx_scatter_kernel<KIND><<<rp.ntiles, RX_THREADS, sizeof(RxScatterSmem), h->stream>>>(in, rp.n, out, offs,
+                                                                                       rp.ntiles, shift, mask);
+  return ej_check_launch(h, "rx_scatter_kernel");
+}
+
+ej_status ej_radix_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
+                        uint32_t shift, uint32_t bits, int digit_kind) {
+  if (rp.n == 0) return EJ_OK;
+  if (bits == 0 || bits > 8 || shift + bits > 32)
+    return ej_fail(h, EJ_ERR_INTERNAL, "radix pass: bad digit (shift %u, bits %u)", shift, bits);
+  if (digit_kind == EJ_DIGIT_VALUE) return radix_pass_kind<EJ_DIGIT_VALUE>(h, rp, in, out, shift, bits);
+  return radix_pass_kind<EJ_DIGIT_HASH>(h, rp, in, out, shift, bits);
+}

@@ -1,0 +1,111 @@
+"""ctypes binding of the engine's C ABI (include/ej.h).
+
+The shared library is built in-tree by :mod:`eating_one_gb300.build`.  Loading
+fails loudly when it is missing: there is no CPU fallback for any join.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB_PATH
+
+EJ_OK = 0
+EJ_ERR_INVALID = 1
+EJ_ERR_CAPACITY = 2
+EJ_ERR_CUDA = 3
+EJ_ERR_NOMEM = 4
+EJ_ERR_TIMEOUT = 5
+EJ_ERR_TOO_LARGE = 6
+EJ_ERR_NO_DEVICE = 7
+EJ_ERR_BUSY = 8
+EJ_ERR_INTERNAL = 9
+
+ALGO = {"hash": 0, "single_hash": 1, "bnl": 2, "hash_index": 3, "sort_index": 4, "left_outer": 5}
+
+EJ_GEN_PERM, EJ_GEN_UNIFORM, EJ_GEN_ZIPF = 0, 1, 2
+
+
+class GenSpec(C.Structure):
+    """Mirror of ej_gen_spec (include/ej_gen.h)."""
+
+    _fields_ = [
+        ("kind", C.c_uint32),
+        ("domain", C.c_uint32),
+        ("seed", C.c_uint64),
+        ("kseed", C.c_uint64),
+        ("n", C.c_uint64),
+        ("dup", C.c_uint32),
+        ("absent_permille", C.c_uint32),
+        ("val_base", C.c_int32),
+        ("absent_base", C.c_int32),
+        ("key_base", C.c_int32),
+        ("reserved", C.c_uint32),
+        ("zipf_s", C.c_double),
+        ("cdf", C.c_void_p),
+    ]
+
+
+_vp, _u64, _pu64, _i32 = C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_int
+
+# name -> argtypes (restype is ej_status = int unless listed in _RESTYPES)
+_SIGS = {
+    "ej_create": [C.c_int, C.POINTER(C.c_void_p)],
+    "ej_destroy": [_vp],
+    "ej_set_stream": [_vp, _vp],
+    "ej_status_name": [_i32],
+    "ej_last_error": [_vp],
+    "ej_scratch_bytes": [_vp],
+    "ej_trim": [_vp],
+    "ej_set_timing": [_vp, _i32],
+    "ej_last_phase_ms": [_vp, C.POINTER(C.c_float)],
+    "ej_set_option": [_vp, _i32, C.c_int64],
+    "ej_hash_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_hash_join_count": [_vp, _vp, _u64, _vp, _u64, _pu64],
+    "ej_hash_join_async": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _vp],
+    "ej_sync_status": [_vp],
+    "ej_single_hash_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_bnl_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_bnl_join_count": [_vp, _vp, _u64, _vp, _u64, _pu64],
+    "ej_hash_index_build": [_vp, _vp, _u64, C.POINTER(C.c_void_p)],
+    "ej_sort_index_build": [_vp, _vp, _u64, C.POINTER(C.c_void_p)],
+    "ej_index_free": [_vp, _vp],
+    "ej_index_join": [_vp, _vp, _vp, _u64, _vp, _u64, _pu64],
+    "ej_index_join_count": [_vp, _vp, _vp, _u64, _pu64],
+    "ej_hash_index_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_sort_index_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_left_outer_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_index_left_outer_join": [_vp, _vp, _vp, _u64, _vp, _u64, _pu64],
+    "ej_star_join3": [_vp, _vp, _vp, _u64, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_join": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_join_host": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_exclusive_scan_u32": [_vp, _vp, _u64, _vp],
+    "ej_generate": [_vp, C.POINTER(GenSpec), _vp],
+    "ej_checksum": [_vp, _vp, _u64, C.c_uint32, _pu64],
+}
+_RESTYPES = {"ej_status_name": C.c_char_p, "ej_last_error": C.c_char_p, "ej_scratch_bytes": C.c_uint64}
+
+_lib = None
+
+
+def exported_names() -> list[str]:
+    return list(_SIGS)
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Load the engine library (building nothing); raises when it is absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            "eating_one_gb300 CUDA library not built (%s missing); run eating_one_gb300.build.build()" % p)
+    lib = C.CDLL(p)
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPES.get(name, C.c_int)
+    if path is None:
+        _lib = lib
+    return lib

@@ -1,0 +1,220 @@
+/*
+ * ej.h - C ABI of the eating_one_gb300 relational join engine (one GB300, sm_103a).
+ *
+ * The reference (yabuta/eating_one) has no library: each join is a standalone
+ * executable whose host `join()` driver allocates device memory, launches
+ * kernels loaded by name from cubins and frees everything again.  This header
+ * is the boundary that replaces those drivers: plain C, plain pointers and
+ * sizes, no C++ or torch types.
+ *
+ * Data layout (bit-identical to the reference structs):
+ *   ej_tuple  == TUPLE  {int key; int val;}          joins/hashJoin_gpu/main_street/tuple.h:43-46
+ *   ej_result == RESULT {int rkey, rval, lkey, lval;} joins/hashJoin_gpu/main_street/tuple.h:48-53
+ * The join attribute is .val; .key is carried through as a row id.
+ * R is the right/build relation (the reference's `rt`, argv[2]) and S is the
+ * left/probe relation (`lt`, argv[1]); every result row holds the R tuple in
+ * (rkey, rval) and the S tuple in (lkey, lval), as join_gpu.cu:104-107 writes.
+ *
+ * Memory: every relation and output pointer is a DEVICE pointer owned by the
+ * caller, except where a function name ends in _host.  Scratch comes from the
+ * handle's arena; nothing the caller passes is freed or replaced (the
+ * reference's presum() frees its input, scan_main.cpp:106-108).
+ *
+ * Output capacity: each join writes min(count, out_cap) rows.  When the join
+ * has more than out_cap results it returns EJ_ERR_CAPACITY and still stores
+ * the full count in *out_count, so the caller can size a buffer and call again
+ * (the count pass of the reference's count -> scan -> join sequence,
+ * hj.cc:997-1069, is exposed separately as the *_count functions).
+ *
+ * Threading: one handle per host thread; a handle is not thread-safe.  All
+ * device work is issued on the handle's stream (ej_set_stream).  Functions
+ * that return a count to the host synchronise that stream before returning.
+ * Errors are status codes; the library never exits, prints or traps.  Device
+ * waits are bounded and report EJ_ERR_TIMEOUT through a device status word.
+ */
+#ifndef EJ_H
+#define EJ_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "ej_gen.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EJ_ABI_VERSION 1
+#define EJ_NULL_KEY INT32_MIN /* NULL sentinel of the left outer join */
+
+typedef struct ej_tuple { int32_t key; int32_t val; } ej_tuple;
+typedef struct ej_result { int32_t rkey; int32_t rval; int32_t lkey; int32_t lval; } ej_result;
+/* one row of the 3-way star join: the two binary result rows of one fact row */
+typedef struct ej_star_result { ej_result d1; ej_result d2; } ej_star_result;
+
+typedef enum ej_status {
+  EJ_OK = 0,
+  EJ_ERR_INVALID = 1,   /* bad argument (null pointer, size out of range) */
+  EJ_ERR_CAPACITY = 2,  /* more results than out_cap; *out_count holds the total */
+  EJ_ERR_CUDA = 3,      /* a CUDA runtime call failed; see ej_last_error */
+  EJ_ERR_NOMEM = 4,     /* device or host allocation failed */
+  EJ_ERR_TIMEOUT = 5,   /* a bounded device wait gave up */
+  EJ_ERR_TOO_LARGE = 6, /* input beyond a documented size limit */
+  EJ_ERR_NO_DEVICE = 7, /* no CUDA device or not an sm_103 device */
+  EJ_ERR_BUSY = 8,      /* serving queue full or admission refused */
+  EJ_ERR_INTERNAL = 9   /* device-side consistency check failed */
+} ej_status;
+
+typedef struct ej_handle ej_handle;
+typedef struct ej_index ej_index;
+typedef void* ej_stream; /* a cudaStream_t; NULL = the legacy default stream */
+
+/* join algorithms of ej_join (mirrors the reference executables) */
+typedef enum ej_algo {
+  EJ_ALGO_HASH = 0,        /* radix-partitioned hash join   (joins/hashJoin_gpu/main_street) */
+  EJ_ALGO_SINGLE_HASH = 1, /* build-side-only hash join     (joins/single-hashjoin/main_street) */
+  EJ_ALGO_BNL = 2,         /* block nested-loop join        (joins/blockJoin_gpu/main_street) */
+  EJ_ALGO_HASH_INDEX = 3,  /* hash-index inner join         (joins/innerJoin_gpu/main_street) */
+  EJ_ALGO_SORT_INDEX = 4,  /* sort-index inner join         (joins/innerJoin_gpu/sort_index/main_street) */
+  EJ_ALGO_LEFT_OUTER = 5   /* left outer join, NULL = INT32_MIN (joins/outerJoin_gpu, see ej_left_outer_join) */
+} ej_algo;
+
+/* ---- handle ------------------------------------------------------------- */
+
+/* Create a handle on `device` (replaces cuInit/cuCtxCreate/cuModuleLoad,
+ * joins/hashJoin_gpu/main_street/hj.cc:213-289). */
+ej_status ej_create(int device, ej_handle** out);
+ej_status ej_destroy(ej_handle* h);
+ej_status ej_set_stream(ej_handle* h, ej_stream stream);
+const char* ej_status_name(ej_status s);
+/* last error text of this handle ("" when none) */
+const char* ej_last_error(const ej_handle* h);
+/* bytes of device scratch the handle holds (arena high-water mark) */
+uint64_t ej_scratch_bytes(const ej_handle* h);
+/* release the handle's cached scratch (the next call re-allocates) */
+ej_status ej_trim(ej_handle* h);
+/* device time of the last join's phases, milliseconds: [0] partition/build,
+ * [1] count + scan, [2] write; like the reference's phase timers
+ * (hj.cc:1194-1237), measured with CUDA events when timing is enabled */
+ej_status ej_set_timing(ej_handle* h, int enable);
+ej_status ej_last_phase_ms(const ej_handle* h, float ms[3]);
+
+/* Tuning knobs (the reference's compile-time #defines, e.g. PARTITION/RADIX/
+ * PART_STANDARD in joins/hashJoin_gpu/main_street/tuple.h:1-16, become runtime
+ * options). */
+typedef enum ej_option {
+  EJ_OPT_PROBE_PARTITION_BITS = 0, /* radix bits of the one S partition pass, 0..8 (0 = probe
+                                      in place); -1 (default) lets the planner choose */
+  EJ_OPT_BUCKET_BITS_DELTA = 1     /* hash-table buckets = 2^(ceil(log2|R|) - 2 + delta),
+                                      delta in -3..3, default 0 */
+} ej_option;
+ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value);
+
+/* ---- equi-joins on device relations ------------------------------------- */
+
+/* Radix-partitioned hash join (replaces join() of joins/hashJoin_gpu/main_street/hj.cc:171-1269:
+ * lcount_partitioning/rcount_partitioning + presum + lpartitioning/rpartitioning,
+ * partitioning.cu:15-271, countPartition :273-293, count/join join_gpu.cu:9-113). */
+ej_status ej_hash_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                       ej_result* out, uint64_t out_cap, uint64_t* out_count);
+/* count pass only (join_gpu.cu:9-66 + presum + getValue, hj.cc:997-1048) */
+ej_status ej_hash_join_count(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                             uint64_t nS, uint64_t* out_count);
+/* Asynchronous form: no host synchronisation; the total count is written to
+ * the device word *d_count and rows beyond out_cap are dropped (the device
+ * status word records EJ_ERR_CAPACITY; read it with ej_sync_status). */
+ej_status ej_hash_join_async(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                             uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* d_count);
+/* synchronise the handle's stream and return (then clear) the device status */
+ej_status ej_sync_status(ej_handle* h);
+
+/* Build-side-only hash join: hash table on R, S probed in input order without
+ * partitioning (replaces joins/single-hashjoin/main_street/singlehash.cc,
+ * partitioning.cu:16-175, join_gpu.cu:10-44). */
+ej_status ej_single_hash_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                              uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count);
+
+/* Block nested-loop equi-join over all |R|x|S| pairs (replaces
+ * joins/blockJoin_gpu/main_street/nestLoopJoin.cc:180-519 and the eval/count/join
+ * kernels of join_gpu.cu:12-120).  Result rows use ej_result, not the
+ * reference's 20-byte JOIN_TUPLE (tuple.h:29-35). */
+ej_status ej_bnl_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                      ej_result* out, uint64_t out_cap, uint64_t* out_count);
+ej_status ej_bnl_join_count(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                            uint64_t nS, uint64_t* out_count);
+
+/* ---- index joins ---------------------------------------------------------- */
+
+/* Index on R's join attribute, built on the device and kept resident until
+ * ej_index_free.  The reference builds both indexes on the CPU and uploads them:
+ * hash index joins/innerJoin_gpu/main_street/inner-idx-bnlj.cc:148-181 (createIndex),
+ * sort index joins/innerJoin_gpu/sort_index/main_street/inner-idx-bnlj.cc:175-217
+ * (qsort + createIndex).  R must stay valid while the index is used. */
+ej_status ej_hash_index_build(ej_handle* h, const ej_tuple* R, uint64_t nR, ej_index** out);
+ej_status ej_sort_index_build(ej_handle* h, const ej_tuple* R, uint64_t nR, ej_index** out);
+ej_status ej_index_free(ej_handle* h, ej_index* idx);
+/* Probe an index with S: inner join (hash index: count.cu:16-48, join_gpu.cu:8-86;
+ * sort index: search/count/join, sort_index/main_street/join_gpu.cu:10-113). */
+ej_status ej_index_join(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS,
+                        ej_result* out, uint64_t out_cap, uint64_t* out_count);
+ej_status ej_index_join_count(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS,
+                              uint64_t* out_count);
+/* Build + probe in one call, timed like the reference (index build then join). */
+ej_status ej_hash_index_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                             uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count);
+ej_status ej_sort_index_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                             uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count);
+
+/* Left outer join preserving S: the inner join plus one row
+ * (EJ_NULL_KEY, EJ_NULL_KEY, s.key, s.val) per S row without a match.  The
+ * reference's joins/outerJoin_gpu/gpu/outer-idx-bnlj.cc:83-168 is named an outer
+ * join but emits no unmatched rows; this entry point gives the outer semantics. */
+ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                             uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count);
+ej_status ej_index_left_outer_join(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS,
+                                   ej_result* out, uint64_t out_cap, uint64_t* out_count);
+
+/* 3-way star join: fact rows (F1[i], F2[i]) share row i; F1[i].val joins D1.val
+ * and F2[i].val joins D2.val; every combination of matches is one row.
+ * The reference has no multi-way join (joins/multi_joins is multi-threaded
+ * CPU code); this entry point composes two index probes. */
+ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tuple* F2, uint64_t nF,
+                        const ej_tuple* D1, uint64_t nD1, const ej_tuple* D2, uint64_t nD2,
+                        ej_star_result* out, uint64_t out_cap, uint64_t* out_count);
+
+/* Generic dispatcher mirroring `./Exe <left> <right>` of the reference drivers. */
+ej_status ej_join(ej_handle* h, ej_algo algo, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
+                  uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count);
+
+/* ---- host-buffer entry points --------------------------------------------- */
+
+/* Same as ej_join, but R, S and out are HOST buffers (pinned memory is fastest):
+ * the call uploads the relations, joins on the device and downloads the rows,
+ * like the reference drivers' cuMemcpyHtoD/DtoH around the kernels
+ * (hj.cc:345-354, :1124).  Device buffers come from the handle's arena. */
+ej_status ej_join_host(ej_handle* h, ej_algo algo, const ej_tuple* R, uint64_t nR,
+                       const ej_tuple* S, uint64_t nS, ej_result* out, uint64_t out_cap,
+                       uint64_t* out_count);
+
+/* ---- prefix scan ----------------------------------------------------------- */
+
+/* Exclusive prefix sum of n uint32 counts into n+1 uint64 offsets (out[n] =
+ * total), single pass with decoupled look-back.  Replaces presum()
+ * (joins/hashJoin_gpu/main_street/scan_main.cpp:38-111), which scans uint32
+ * in place, pads to 2048/2^20 multiples and frees its input. */
+ej_status ej_exclusive_scan_u32(ej_handle* h, const uint32_t* in, uint64_t n, uint64_t* out);
+
+/* ---- inputs and checks --------------------------------------------------- */
+
+/* Fill a device relation from a generator spec (see ej_gen.h).  For Zipf specs
+ * with s > 0, spec->cdf may be NULL: the library builds the CDF itself. */
+ej_status ej_generate(ej_handle* h, const ej_gen_spec* spec, ej_tuple* out);
+/* Order-independent checksum of rows (sum of a 64-bit mix per row; the same
+ * function as the oracle's), for comparing result multisets without sorting. */
+ej_status ej_checksum(ej_handle* h, const void* rows, uint64_t nrows, uint32_t words_per_row,
+                      uint64_t* out_sum);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EJ_H */

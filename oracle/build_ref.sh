@@ -1,0 +1,41 @@
+#!/bin/sh
+# build_ref.sh - compile the reference's own CPU join programs from their
+# sources (read in place, never copied) into oracle/_ref/.  TEST
+# INFRASTRUCTURE ONLY: the binaries pin the oracle to the reference's output
+# (tests/golden/make_golden.py).  Needs the reference checkout; does nothing
+# without it.  Outputs only into oracle/_ref/.
+#
+#   oracle/_ref/join_ori_{bnlj,hj,inner,outer}   joins/join_ori/*.cc as written
+#                                                (read files R and S in the CWD)
+#   oracle/_ref/{hash,inner,sortindex,block}_cpu joins/CPU_JOIN/*/ with
+#                                                oracle/ref_shim.cpp injecting inputs
+set -e
+REF=${EJ_REFERENCE:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -d "$REF/joins" ]; then
+  echo "build_ref.sh: no reference at $REF, nothing built" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+CXX=${CXX:-g++}
+FLAGS="-O2 -w"
+
+J="$REF/joins/join_ori"
+$CXX $FLAGS -I"$J" "$J/bnlj.cc" -o "$OUT/join_ori_bnlj"
+$CXX $FLAGS -I"$J" "$J/hj.cc" -o "$OUT/join_ori_hj"
+$CXX $FLAGS -I"$J" "$J/inner-idx-bnlj.cc" -o "$OUT/join_ori_inner"
+$CXX $FLAGS -I"$J" "$J/outer-idx-bnlj.cc" -o "$OUT/join_ori_outer"
+
+C="$REF/joins/CPU_JOIN"
+shim() {  # name source-dir source-file right-global left-global result-global
+  $CXX $FLAGS -c -include "$HERE/ref_prelude.h" -I"$C/$2" "$C/$2/$3" -o "$OUT/$1.ref.o"
+  $CXX $FLAGS -c -DEJ_REF_RIGHT="$4" -DEJ_REF_LEFT="$5" ${6:+-DEJ_REF_RESULT=$6} "$HERE/ref_shim.cpp" -o "$OUT/$1.shim.o"
+  $CXX "$OUT/$1.ref.o" "$OUT/$1.shim.o" -o "$OUT/$1" -lm -lpthread
+  rm -f "$OUT/$1.ref.o" "$OUT/$1.shim.o"
+}
+shim hash_cpu hash_cpu hj.cc rt lt
+shim inner_cpu inner_cpu inner-idx-bnlj.cc rt lt jt
+shim sortindex_cpu sortIndex_cpu inner-idx-bnlj.cc rt lt jt
+shim block_cpu block_cpu nestLoopJoin.cc Tright Tleft Tjoin
+echo "built reference programs into $OUT"

@@ -1,0 +1,393 @@
+/*
+ * ej_oracle.c - CPU restatement of the reference's join algorithms.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the CUDA join
+ * engine: the tests, the smoke check and the CPU-baseline leg of the bench call
+ * it as a checker.  The engine never links it, and nothing in the engine falls
+ * back to it.
+ *
+ * Each join below follows one reference program loop for loop, but takes the
+ * relations as arguments and materialises every result row (the reference
+ * programs generate their own time-seeded inputs and only print a count).
+ * Paths are relative to the reference project root.
+ *
+ * Conventions shared with the reference and the engine:
+ *   TUPLE  {int key; int val;}   - .val is the join attribute, .key a row id
+ *                                  (joins/hashJoin_gpu/main_street/tuple.h:43-46)
+ *   RESULT {rkey, rval, lkey, lval} - r* from the right/build relation R,
+ *                                  l* from the left/probe relation S
+ *                                  (joins/hashJoin_gpu/main_street/join_gpu.cu:104-107)
+ *
+ * Deliberate differences from the reference sources, none of which changes
+ * the result multiset of a correct join:
+ *   - hash_cpu's match loop reads hrt[llocation[i]+j] / hlt[rlocation[i]+k]
+ *     (swapped indices, joins/CPU_JOIN/hash_cpu/hj.cc:220-223); the
+ *     restatement takes r-fields from R and l-fields from S as the GPU join does.
+ *   - bucket indices use the unsigned value (uint32)val % buckets; the
+ *     reference's signed `val % N` would index out of bounds for negative keys.
+ *   - sortIndex_cpu's upward duplicate walk reads Bucket[bidx+1] even when
+ *     bidx+1 == right (joins/CPU_JOIN/sortIndex_cpu/inner-idx-bnlj.cc:226-227);
+ *     the restatement checks the bound first.
+ *   - counts and offsets are 64-bit (the reference uses int/uint).
+ *   - the left outer join and the 3-way star join have no reference
+ *     implementation (joins/outerJoin_gpu computes an inner join); their
+ *     semantics here are defined by this file: outer = inner join plus
+ *     (INT32_MIN, INT32_MIN, s.key, s.val) for every unmatched S row;
+ *     star = both dimension probes of each fact row, cross product of matches.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include "ej_gen.h"
+
+typedef struct { int32_t key, val; } ejo_tuple;
+typedef struct { int32_t rkey, rval, lkey, lval; } ejo_result;
+typedef struct { ejo_result d1, d2; } ejo_star_result;
+typedef struct { int32_t adr, val; } ejo_bucket; /* BUCKET, CPU field order (hash_cpu/tuple.h:28-32) */
+
+#define EJO_NULL INT32_MIN
+
+static inline void emit(ejo_result* out, uint64_t cap, uint64_t n, const ejo_tuple* r, const ejo_tuple* s) {
+  if (n < cap) {
+    out[n].rkey = r->key;
+    out[n].rval = r->val;
+    out[n].lkey = s->key;
+    out[n].lval = s->val;
+  }
+}
+
+/* ---------------------------------------------------------------------------
+ * Partitioned hash join: joins/CPU_JOIN/hash_cpu/hj.cc
+ *   createPart (hj.cc:116-183): histogram of val % NB_BKTENT, exclusive prefix
+ *   (rlocation/llocation), scatter into hrt/hlt, for R then for S;
+ *   match loop (hj.cc:216-228): per bucket, every S row against every R row.
+ * nb_bktent = NB_BKTENT (2^20 in hash_cpu/tuple.h:1).
+ * Returns the number of matches; writes min(matches, cap) rows.
+ * ------------------------------------------------------------------------- */
+static int partition_side(const ejo_tuple* in, uint64_t n, uint32_t nb, ejo_tuple* out,
+                          uint64_t* loc, uint64_t* cnt) {
+  memset(cnt, 0, sizeof(uint64_t) * nb);
+  for (uint64_t i = 0; i < n; i++) cnt[(uint32_t)in[i].val % nb]++;
+  loc[0] = 0;
+  for (uint32_t i = 1; i < nb; i++) loc[i] = loc[i - 1] + cnt[i - 1];
+  memset(cnt, 0, sizeof(uint64_t) * nb);
+  for (uint64_t i = 0; i < n; i++) {
+    uint32_t idx = (uint32_t)in[i].val % nb;
+    out[loc[idx] + cnt[idx]] = in[i];
+    cnt[idx]++;
+  }
+  return 0;
+}
+
+uint64_t ejo_hash_join(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS,
+                       ejo_result* out, uint64_t cap, uint32_t nb_bktent) {
+  if (nb_bktent == 0) nb_bktent = 1u << 20;
+  ejo_tuple* hrt = (ejo_tuple*)malloc(sizeof(ejo_tuple) * (nR ? nR : 1));
+  ejo_tuple* hlt = (ejo_tuple*)malloc(sizeof(ejo_tuple) * (nS ? nS : 1));
+  uint64_t* rloc = (uint64_t*)malloc(sizeof(uint64_t) * nb_bktent);
+  uint64_t* rcnt = (uint64_t*)malloc(sizeof(uint64_t) * nb_bktent);
+  uint64_t* lloc = (uint64_t*)malloc(sizeof(uint64_t) * nb_bktent);
+  uint64_t* lcnt = (uint64_t*)malloc(sizeof(uint64_t) * nb_bktent);
+  uint64_t n = 0;
+  if (!hrt || !hlt || !rloc || !rcnt || !lloc || !lcnt) { n = UINT64_MAX; goto done; }
+  partition_side(R, nR, nb_bktent, hrt, rloc, rcnt);
+  partition_side(S, nS, nb_bktent, hlt, lloc, lcnt);
+  for (uint32_t i = 0; i < nb_bktent; i++) {
+    for (uint64_t j = 0; j < lcnt[i]; j++) {
+      const ejo_tuple* s = &hlt[lloc[i] + j];
+      for (uint64_t k = 0; k < rcnt[i]; k++) {
+        const ejo_tuple* r = &hrt[rloc[i] + k];
+        if (s->val == r->val) { emit(out, cap, n, r, s); n++; }
+      }
+    }
+  }
+done:
+  free(hrt); free(hlt); free(rloc); free(rcnt); free(lloc); free(lcnt);
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * Hash-index inner join: joins/CPU_JOIN/inner_cpu/inner-idx-bnlj.cc
+ *   index (:142-166): idxcount[val % NB_BUCKET]++, Buck_array = exclusive
+ *   prefix (-1 for empty buckets), Bucket[] = {val, adr=row} grouped by bucket;
+ *   probe (:174-185): per S row, scan its bucket comparing val.
+ * nb_bucket = NB_BUCKET (2^27 in inner_cpu/tuple.h:1).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  uint32_t nb;
+  int64_t* buck_array; /* start of bucket, -1 when empty */
+  uint64_t* idxcount;
+  ejo_bucket* bucket;
+} ejo_hash_index;
+
+static int hash_index_build(const ejo_tuple* R, uint64_t nR, uint32_t nb, ejo_hash_index* ix) {
+  ix->nb = nb;
+  ix->buck_array = (int64_t*)malloc(sizeof(int64_t) * nb);
+  ix->idxcount = (uint64_t*)calloc(nb, sizeof(uint64_t));
+  ix->bucket = (ejo_bucket*)malloc(sizeof(ejo_bucket) * (nR ? nR : 1));
+  if (!ix->buck_array || !ix->idxcount || !ix->bucket) return -1;
+  for (uint64_t i = 0; i < nR; i++) ix->idxcount[(uint32_t)R[i].val % nb]++;
+  uint64_t count = 0;
+  for (uint32_t i = 0; i < nb; i++) {
+    ix->buck_array[i] = ix->idxcount[i] == 0 ? -1 : (int64_t)count;
+    count += ix->idxcount[i];
+  }
+  memset(ix->idxcount, 0, sizeof(uint64_t) * nb);
+  for (uint64_t i = 0; i < nR; i++) {
+    uint32_t idx = (uint32_t)R[i].val % nb;
+    ejo_bucket* b = &ix->bucket[ix->buck_array[idx] + ix->idxcount[idx]];
+    b->val = R[i].val;
+    b->adr = (int32_t)i;
+    ix->idxcount[idx]++;
+  }
+  return 0;
+}
+
+static void hash_index_free(ejo_hash_index* ix) {
+  free(ix->buck_array); free(ix->idxcount); free(ix->bucket);
+}
+
+/* matches of one probe row; emits from position n, returns the new n */
+static uint64_t hash_index_probe_row(const ejo_hash_index* ix, const ejo_tuple* R, const ejo_tuple* s,
+                                     ejo_result* out, uint64_t cap, uint64_t n) {
+  uint32_t hash = (uint32_t)s->val % ix->nb;
+  uint64_t cnt = ix->idxcount[hash];
+  for (uint64_t i = 0; i < cnt; i++) {
+    const ejo_bucket* b = &ix->bucket[ix->buck_array[hash] + i];
+    if (b->val == s->val) { emit(out, cap, n, &R[b->adr], s); n++; }
+  }
+  return n;
+}
+
+uint64_t ejo_hash_index_join(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS,
+                             ejo_result* out, uint64_t cap, uint32_t nb_bucket) {
+  if (nb_bucket == 0) nb_bucket = 1u << 27;
+  ejo_hash_index ix;
+  uint64_t n = 0;
+  if (hash_index_build(R, nR, nb_bucket, &ix) != 0) { hash_index_free(&ix); return UINT64_MAX; }
+  for (uint64_t j = 0; j < nS; j++) n = hash_index_probe_row(&ix, R, &S[j], out, cap, n);
+  hash_index_free(&ix);
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * Sort-index inner join: joins/CPU_JOIN/sortIndex_cpu/inner-idx-bnlj.cc
+ *   createIndex (:129-146): Bucket[i] = {val, adr=i}, recursive quicksort on
+ *   val (:106-127, middle pivot, Hoare-style crossing scans);
+ *   search (:163-174): binary search that stops on the first equal element;
+ *   probe (:212-237): walk equal values downward from the hit, then upward.
+ * ------------------------------------------------------------------------- */
+static void sort_index_qsort(ejo_bucket* b, int64_t p, int64_t q) {
+  /* explicit stack instead of recursion; same partition step as the reference */
+  int64_t stack[2 * 64 * 2];
+  int top = 0;
+  stack[top++] = p; stack[top++] = q;
+  while (top > 0) {
+    q = stack[--top]; p = stack[--top];
+    for (;;) {
+      int64_t i = p, j = q;
+      int32_t pivot = b[(p + q) / 2].val;
+      for (;;) {
+        while (b[i].val < pivot) i++;
+        while (pivot < b[j].val) j--;
+        if (i >= j) break;
+        ejo_bucket t = b[i]; b[i] = b[j]; b[j] = t;
+        i++; j--;
+      }
+      /* sub-ranges [p, i-1] and [j+1, q]; recurse on the smaller one first */
+      int64_t lp = p, lq = i - 1, rp = j + 1, rq = q;
+      int has_l = p < i - 1, has_r = j + 1 < q;
+      if (has_l && has_r) {
+        if (lq - lp < rq - rp) { stack[top++] = rp; stack[top++] = rq; p = lp; q = lq; }
+        else { stack[top++] = lp; stack[top++] = lq; p = rp; q = rq; }
+        continue;
+      }
+      if (has_l) { p = lp; q = lq; continue; }
+      if (has_r) { p = rp; q = rq; continue; }
+      break;
+    }
+  }
+}
+
+static int64_t sort_index_search(const ejo_bucket* b, int32_t num, uint64_t right) {
+  int64_t m, l = 0, r = (int64_t)right - 1;
+  do {
+    m = (l + r) / 2;
+    if (num < b[m].val) r = m - 1; else l = m + 1;
+  } while (l <= r && num != b[m].val);
+  return m;
+}
+
+uint64_t ejo_sort_index_join(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS,
+                             ejo_result* out, uint64_t cap) {
+  if (nR == 0) return 0;
+  ejo_bucket* b = (ejo_bucket*)malloc(sizeof(ejo_bucket) * nR);
+  if (!b) return UINT64_MAX;
+  for (uint64_t i = 0; i < nR; i++) { b[i].val = R[i].val; b[i].adr = (int32_t)i; }
+  sort_index_qsort(b, 0, (int64_t)nR - 1);
+  uint64_t n = 0;
+  for (uint64_t j = 0; j < nS; j++) {
+    const ejo_tuple* s = &S[j];
+    int64_t bidx = sort_index_search(b, s->val, nR);
+    int64_t x = bidx;
+    while (b[x].val == s->val) {
+      emit(out, cap, n, &R[b[x].adr], s); n++;
+      if (x == 0) break;
+      x--;
+    }
+    x = bidx + 1;
+    while (x < (int64_t)nR && b[x].val == s->val) {
+      emit(out, cap, n, &R[b[x].adr], s); n++;
+      x++;
+    }
+  }
+  free(b);
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * Block nested-loop join: joins/CPU_JOIN/block_cpu/nestLoopJoin.cc:61-77
+ *   every left (S) row against every right (R) row, equality on val.
+ * ------------------------------------------------------------------------- */
+uint64_t ejo_bnl_join(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS,
+                      ejo_result* out, uint64_t cap) {
+  uint64_t n = 0;
+  for (uint64_t i = 0; i < nS; i++)
+    for (uint64_t j = 0; j < nR; j++)
+      if (S[i].val == R[j].val) { emit(out, cap, n, &R[j], &S[i]); n++; }
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * Left outer join (semantics defined here; see header): hash-index probe as in
+ * inner_cpu, plus one (INT32_MIN, INT32_MIN, s.key, s.val) row per unmatched S row.
+ * ------------------------------------------------------------------------- */
+uint64_t ejo_left_outer_join(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS,
+                             ejo_result* out, uint64_t cap, uint32_t nb_bucket) {
+  if (nb_bucket == 0) nb_bucket = 1u << 27;
+  ejo_hash_index ix;
+  uint64_t n = 0;
+  if (hash_index_build(R, nR, nb_bucket, &ix) != 0) { hash_index_free(&ix); return UINT64_MAX; }
+  ejo_tuple null_r = {EJO_NULL, EJO_NULL};
+  for (uint64_t j = 0; j < nS; j++) {
+    uint64_t before = n;
+    n = hash_index_probe_row(&ix, R, &S[j], out, cap, n);
+    if (n == before) { emit(out, cap, n, &null_r, &S[j]); n++; }
+  }
+  hash_index_free(&ix);
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * 3-way star join (semantics defined here; see header): fact rows F1[i], F2[i]
+ * (same row id, two foreign-key columns) joined with D1 on F1.val and with D2
+ * on F2.val; every pair of matches is one output row {d1-part, d2-part}.
+ * ------------------------------------------------------------------------- */
+uint64_t ejo_star_join3(const ejo_tuple* F1, const ejo_tuple* F2, uint64_t nF,
+                        const ejo_tuple* D1, uint64_t nD1, const ejo_tuple* D2, uint64_t nD2,
+                        ejo_star_result* out, uint64_t cap, uint32_t nb_bucket) {
+  if (nb_bucket == 0) nb_bucket = 1u << 20;
+  ejo_hash_index i1, i2;
+  uint64_t n = 0;
+  int ok = hash_index_build(D1, nD1, nb_bucket, &i1) == 0;
+  ok = (hash_index_build(D2, nD2, nb_bucket, &i2) == 0) && ok;
+  if (!ok) { hash_index_free(&i1); hash_index_free(&i2); return UINT64_MAX; }
+  for (uint64_t f = 0; f < nF; f++) {
+    uint32_t h1 = (uint32_t)F1[f].val % nb_bucket, h2 = (uint32_t)F2[f].val % nb_bucket;
+    for (uint64_t a = 0; a < i1.idxcount[h1]; a++) {
+      const ejo_bucket* b1 = &i1.bucket[i1.buck_array[h1] + a];
+      if (b1->val != F1[f].val) continue;
+      for (uint64_t c = 0; c < i2.idxcount[h2]; c++) {
+        const ejo_bucket* b2 = &i2.bucket[i2.buck_array[h2] + c];
+        if (b2->val != F2[f].val) continue;
+        if (n < cap) {
+          const ejo_tuple* d1 = &D1[b1->adr];
+          const ejo_tuple* d2 = &D2[b2->adr];
+          out[n].d1.rkey = d1->key; out[n].d1.rval = d1->val;
+          out[n].d1.lkey = F1[f].key; out[n].d1.lval = F1[f].val;
+          out[n].d2.rkey = d2->key; out[n].d2.rval = d2->val;
+          out[n].d2.lkey = F2[f].key; out[n].d2.lval = F2[f].val;
+        }
+        n++;
+      }
+    }
+  }
+  hash_index_free(&i1); hash_index_free(&i2);
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * Count-only hash join (no materialisation): the count pass of hash_cpu for
+ * sizes whose result does not fit in host memory.
+ * ------------------------------------------------------------------------- */
+uint64_t ejo_hash_join_count(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS,
+                             uint32_t nb_bucket) {
+  if (nb_bucket == 0) nb_bucket = 1u << 20;
+  ejo_hash_index ix;
+  uint64_t n = 0;
+  if (hash_index_build(R, nR, nb_bucket, &ix) != 0) { hash_index_free(&ix); return UINT64_MAX; }
+  for (uint64_t j = 0; j < nS; j++) {
+    uint32_t hash = (uint32_t)S[j].val % nb_bucket;
+    for (uint64_t i = 0; i < ix.idxcount[hash]; i++)
+      n += ix.bucket[ix.buck_array[hash] + i].val == S[j].val;
+  }
+  hash_index_free(&ix);
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * Inputs and result canonicalisation
+ * ------------------------------------------------------------------------- */
+void ejo_generate(const ej_gen_spec* sp, ejo_tuple* out) {
+  for (uint64_t i = 0; i < sp->n; i++) {
+    out[i].key = (int32_t)((uint32_t)sp->key_base + (uint32_t)i);
+    out[i].val = ej_gen_val(sp, i);
+  }
+}
+
+void ejo_zipf_cdf(double s, uint32_t n, double* cdf) {
+  double total = 0.0;
+  for (uint32_t k = 0; k < n; k++) { total += pow((double)(k + 1u), -s); cdf[k] = total; }
+  for (uint32_t k = 0; k < n; k++) cdf[k] = cdf[k] / total;
+  if (n) cdf[n - 1] = 1.0;
+}
+
+static int cmp_result(const void* a, const void* b) {
+  const int32_t* x = (const int32_t*)a;
+  const int32_t* y = (const int32_t*)b;
+  for (int i = 0; i < 4; i++) {
+    if (x[i] < y[i]) return -1;
+    if (x[i] > y[i]) return 1;
+  }
+  return 0;
+}
+
+/* canonical order: lexicographic on (rkey, rval, lkey, lval) as signed int32 */
+void ejo_canon_sort(ejo_result* r, uint64_t n) { qsort(r, n, sizeof(ejo_result), cmp_result); }
+
+static int cmp_result8(const void* a, const void* b) {
+  const int32_t* x = (const int32_t*)a;
+  const int32_t* y = (const int32_t*)b;
+  for (int i = 0; i < 8; i++) {
+    if (x[i] < y[i]) return -1;
+    if (x[i] > y[i]) return 1;
+  }
+  return 0;
+}
+
+void ejo_canon_sort_star(ejo_star_result* r, uint64_t n) {
+  qsort(r, n, sizeof(ejo_star_result), cmp_result8);
+}
+
+/* order-independent checksum of 16-byte rows: sum over rows of a 64-bit mix */
+uint64_t ejo_checksum(const int32_t* words, uint64_t nrows, uint32_t words_per_row) {
+  uint64_t sum = 0;
+  for (uint64_t i = 0; i < nrows; i++) {
+    uint64_t h = 0x243F6A8885A308D3ull;
+    for (uint32_t w = 0; w < words_per_row; w++)
+      h = ej_splitmix64(h ^ (uint64_t)(uint32_t)words[i * words_per_row + w]);
+    sum += h;
+  }
+  return sum;
+}

@@ -1,0 +1,243 @@
+"""Parity of every join entry point against the CPU oracle (exact result multisets).
+
+Each test runs the CUDA path through the C ABI (libeating_one.so via ctypes)
+and compares its rows, after canonical sorting, with the oracle's restatement
+of the reference algorithm on the same seeded inputs.  Integer joins must be
+bit-exact: there is no tolerance anywhere in this file.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from eating_one_gb300 import native
+from eating_one_gb300.engine import JoinError
+from eating_one_gb300.workloads import make_spec, workload
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+INT_MIN, INT_MAX = -(2 ** 31), 2 ** 31 - 1
+
+
+def dev(a: np.ndarray) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.int32)).cuda()
+
+
+def same_multiset(gpu_rows: torch.Tensor, ref_rows: np.ndarray) -> None:
+    g = O.canon(gpu_rows.cpu().numpy())
+    r = O.canon(ref_rows)
+    assert g.shape == r.shape, (g.shape, r.shape)
+    assert np.array_equal(g, r)
+
+
+def rel(rng, n, lo, hi, key_base=0):
+    a = np.empty((n, 2), dtype=np.int32)
+    a[:, 0] = np.arange(key_base, key_base + n, dtype=np.int64).astype(np.int32)
+    a[:, 1] = rng.integers(lo, hi, size=n, dtype=np.int64).astype(np.int32)
+    return a
+
+
+ORACLE = {
+    "hash": O.hash_join,
+    "single_hash": O.hash_join,
+    "hash_index": O.hash_index_join,
+    "sort_index": O.sort_index_join,
+    "bnl": O.bnl_join,
+    "left_outer": O.left_outer_join,
+}
+
+CASES = [  # (nR, nS, key range) - unique-ish, many-to-many, heavy duplicates, ragged sizes
+    (1000, 5000, (0, 1 << 20)),
+    (4097, 8191, (0, 512)),
+    (3, 100000, (0, 4)),
+    (65536, 65536, (INT_MIN, INT_MAX)),
+    (12345, 54321, (-1000, 1000)),
+    (1, 1, (7, 8)),
+]
+
+
+@pytest.mark.parametrize("algo", list(ORACLE))
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_small_parity(engine, algo, case):
+    nR, nS, (lo, hi) = CASES[case]
+    rng = np.random.default_rng(1000 + case)
+    R, S = rel(rng, nR, lo, hi), rel(rng, nS, lo, hi, key_base=nR)
+    got = engine.join(algo, dev(R), dev(S))
+    same_multiset(got, ORACLE[algo](R, S))
+
+
+@pytest.mark.parametrize("algo", list(ORACLE))
+def test_empty_relations(engine, algo):
+    rng = np.random.default_rng(7)
+    R = rel(rng, 100, 0, 10)
+    empty = np.zeros((0, 2), dtype=np.int32)
+    for a, b in ((empty, R), (R, empty), (empty, empty)):
+        got = engine.join(algo, dev(a), dev(b))
+        assert got.shape[0] == len(ORACLE[algo](a, b))
+
+
+def test_extreme_keys(engine):
+    vals = np.array([INT_MIN, INT_MIN + 1, -1, 0, 1, INT_MAX - 1, INT_MAX], dtype=np.int32)
+    R = np.stack([np.arange(len(vals) * 3, dtype=np.int32), np.repeat(vals, 3)], axis=1)
+    S = np.stack([np.arange(100, 100 + len(vals) * 2, dtype=np.int32), np.tile(vals, 2)], axis=1)
+    for algo in ORACLE:
+        same_multiset(engine.join(algo, dev(R), dev(S)), ORACLE[algo](R, S))
+
+
+@pytest.mark.parametrize("pb", [1, 3, 6, 8])
+def test_partitioned_probe(engine, pb):
+    """Force the S radix-partition pass (taken automatically only for tables beyond L2)."""
+    rng = np.random.default_rng(pb)
+    R, S = rel(rng, 50000, 0, 30000), rel(rng, 200003, 0, 40000, key_base=50000)
+    engine.set_option("partition_bits", pb)
+    try:
+        got_hash = engine.join("hash", dev(R), dev(S))
+        got_outer = engine.join("left_outer", dev(R), dev(S))
+    finally:
+        engine.set_option("partition_bits", -1)
+    same_multiset(got_hash, O.hash_join(R, S))
+    same_multiset(got_outer, O.left_outer_join(R, S))
+
+
+@pytest.mark.parametrize("delta", [-3, 3])
+def test_bucket_sizes(engine, delta):
+    rng = np.random.default_rng(11)
+    R, S = rel(rng, 30000, 0, 5000), rel(rng, 70000, 0, 6000, key_base=30000)
+    engine.set_option("bucket_bits_delta", delta)
+    try:
+        got = engine.join("hash", dev(R), dev(S))
+    finally:
+        engine.set_option("bucket_bits_delta", 0)
+    same_multiset(got, O.hash_join(R, S))
+
+
+def test_c1_full_size(engine):
+    """Configuration C1 at full size: 2^20 unique R keys, 2^22 uniform S keys."""
+    w = workload("c1")
+    R, S = O.generate(w["R"]), O.generate(w["S"])
+    Rd, Sd = engine.generate(w["R"]), engine.generate(w["S"])
+    assert np.array_equal(Rd.cpu().numpy(), R) and np.array_equal(Sd.cpu().numpy(), S)
+    got = engine.hash_join(Rd, Sd)
+    assert got.shape[0] == len(S)  # every S key matches exactly one R tuple
+    same_multiset(got, O.hash_join(R, S))
+    assert engine.checksum(got) == O.checksum(O.hash_join(R, S))
+
+
+@pytest.mark.parametrize("s", ["0.0", "0.75", "1.0"])
+def test_c3_shape_reduced(engine, s):
+    """Configuration C3's shape (x4 duplicated R keys, Zipf S with 10% absent) at 1/64 size."""
+    w = workload("c3_s" + s, scale=6)
+    R, S = O.generate(w["R"]), O.generate(w["S"])
+    Rd, Sd = engine.generate(w["R"]), engine.generate(w["S"])
+    assert np.array_equal(Sd.cpu().numpy(), S)
+    got = engine.hash_join(Rd, Sd)
+    same_multiset(got, O.hash_join(R, S))
+
+
+def test_capacity_and_guard(engine):
+    rng = np.random.default_rng(3)
+    R, S = rel(rng, 5000, 0, 100), rel(rng, 20000, 0, 100, key_base=5000)
+    total = len(O.hash_join(R, S))
+    cap = total // 3
+    guard = 1000
+    out = torch.full((cap + guard, 4), -7, dtype=torch.int32, device="cuda")
+    with pytest.raises(JoinError) as ei:
+        engine.hash_join(dev(R), dev(S), out=out[:cap])
+    assert ei.value.status == native.EJ_ERR_CAPACITY
+    assert torch.all(out[cap:] == -7)  # nothing written past out_cap
+    assert engine.count("hash", dev(R), dev(S)) == total
+
+
+def test_index_reuse_and_count(engine):
+    rng = np.random.default_rng(5)
+    R = rel(rng, 40000, 0, 20000)
+    S1, S2 = rel(rng, 100000, 0, 30000, key_base=40000), rel(rng, 7777, -5, 25000, key_base=140000)
+    for kind, ref in (("hash", O.hash_index_join), ("sort", O.sort_index_join)):
+        ix = engine.build_index(kind, dev(R))
+        try:
+            same_multiset(ix.join(dev(S1)), ref(R, S1))
+            same_multiset(ix.join(dev(S2)), ref(R, S2))
+            assert ix.count(dev(S1)) == len(ref(R, S1))
+            same_multiset(ix.left_outer_join(dev(S2)), O.left_outer_join(R, S2))
+        finally:
+            ix.free()
+
+
+def test_star_join(engine):
+    w = workload("c4_star", scale=8)
+    t = {k: O.generate(v) for k, v in w.items()}
+    got = engine.star_join3(*(dev(t[k]) for k in ("F1", "F2", "D1", "D2")))
+    ref = O.star_join3(t["F1"], t["F2"], t["D1"], t["D2"])
+    assert len(ref) == len(t["F1"])  # 100% foreign-key hits, unique dimension keys
+    same_multiset(got, ref)
+    # many-to-many dimensions
+    rng = np.random.default_rng(9)
+    F1, F2 = rel(rng, 3000, 0, 50), rel(rng, 3000, 0, 40)
+    F2[:, 0] = F1[:, 0]
+    D1, D2 = rel(rng, 200, 0, 60), rel(rng, 300, 0, 45)
+    same_multiset(engine.star_join3(dev(F1), dev(F2), dev(D1), dev(D2)), O.star_join3(F1, F2, D1, D2))
+
+
+def test_host_buffer_path(engine):
+    rng = np.random.default_rng(21)
+    R, S = rel(rng, 30000, 0, 50000), rel(rng, 90000, 0, 60000, key_base=30000)
+    ref = O.hash_join(R, S)
+    out = np.zeros((len(ref) + 10, 4), dtype=np.int32)
+    n = engine.join_host("hash", R, S, out)
+    assert n == len(ref)
+    assert np.array_equal(O.canon(out[:n]), O.canon(ref))
+
+
+def test_async_hash_join(engine):
+    rng = np.random.default_rng(22)
+    R, S = rel(rng, 20000, 0, 30000), rel(rng, 80000, 0, 30000, key_base=20000)
+    ref = O.hash_join(R, S)
+    out = torch.empty((len(ref), 4), dtype=torch.int32, device="cuda")
+    d_count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    engine.hash_join_async(dev(R), dev(S), out, d_count)
+    assert engine.sync_status() == native.EJ_OK
+    assert int(d_count.item()) == len(ref)
+    same_multiset(out, ref)
+
+
+@pytest.mark.parametrize("n", [0, 1, 4095, 4096, 4097, 1 << 20, 3_000_001])
+def test_exclusive_scan(engine, n):
+    rng = np.random.default_rng(n)
+    x = rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
+    got = engine.exclusive_scan_u32(torch.from_numpy(x.view(np.int32)).cuda()).cpu().numpy().view(np.uint64)
+    ref = np.zeros(n + 1, dtype=np.uint64)
+    ref[1:] = np.cumsum(x.astype(np.uint64))
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("name", ["c1", "c2", "c3_s0.0", "c3_s0.75", "c3_s1.0", "c4", "c4_star"])
+def test_device_generator_matches_host(engine, name):
+    for side, spec in workload(name, scale=8).items():
+        assert np.array_equal(engine.generate(spec).cpu().numpy(), O.generate(spec)), (name, side)
+
+
+def test_checksum_matches_oracle(engine):
+    rng = np.random.default_rng(4)
+    rows = rng.integers(INT_MIN, INT_MAX, size=(100003, 4), dtype=np.int64).astype(np.int32)
+    assert engine.checksum(dev(rows)) == O.checksum(rows)
+    star = rng.integers(INT_MIN, INT_MAX, size=(5001, 8), dtype=np.int64).astype(np.int32)
+    assert engine.checksum(dev(star)) == O.checksum(star)
+
+
+def test_bnl_c2_shape_reduced(engine):
+    w = workload("c2", scale=2)
+    R, S = O.generate(w["R"]), O.generate(w["S"])
+    got = engine.join("bnl", dev(R), dev(S))
+    same_multiset(got, O.hash_join(R, S))
+    assert engine.count("bnl", dev(R), dev(S)) == len(got)
+
+
+def test_bnl_unaligned_probe_side(engine):
+    """S not 16-byte aligned takes the plain-load staging path instead of TMA."""
+    rng = np.random.default_rng(8)
+    R, S = rel(rng, 5000, 0, 3000), rel(rng, 20001, 0, 3000, key_base=5000)
+    Sd = dev(np.concatenate([np.zeros((1, 2), np.int32), S]))[1:]
+    assert Sd.data_ptr() % 16 == 8
+    same_multiset(engine.join("bnl", dev(R), Sd), O.bnl_join(R, S))
