@@ -1,0 +1,363 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 join engine on the skewed hash-join workload.
+
+One step = the three hash joins of configuration C3 (R = 2^26 tuples holding
+2^24 distinct keys x4, S = 2^28 tuples with Zipf(s) keys over R's keys, 10% of
+S from an absent key range, s in {0, 0.75, 1}), each run end to end on the
+device: R table build (LSD radix passes + bucket starts), one S radix pass,
+count pass, look-back scan, write pass of every result row.  Inputs are
+generated on the device with seeded integer generators (synthetic data;
+every input is far larger than the 126 MB L2).
+
+Printed (rank 0, one JSON line):
+  value      input tuples/s of the whole job (all ranks), inputs resident in HBM
+  e2e        the same metric through ej_join_host (the C ABI call with host
+             buffers: host->device copies of R and S and the device->host copy
+             of every result row inside the timed region)
+  roofline   the dominant kernel's algorithmic bytes / its event-timed duration
+  join_roofline  algorithmic bytes of the whole join, 24(|R|+|S|) + 16|out|,
+             over the step time - the fraction of the HBM roofline
+  cpu_baseline   the oracle's restatement of the reference CPU hash join
+             (joins/CPU_JOIN/hash_cpu) timed on a 1/16-size sample, rank 0
+
+`--impl reference` times that CPU implementation alone (the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "join input tuples/s and % HBM roofline (bit-exact); batched vs per-launch p50/p99"
+UNIT = "tuples/s"
+VARIANTS = ["c3_s0.0", "c3_s0.75", "c3_s1.0"]
+WORKLOAD = ("C3 skewed hash join x3: R=2^26 (2^24 keys x4) join S=2^28 Zipf(s) over R's keys, "
+            "10% absent keys, s in {0, 0.75, 1}; one step = the three joins")
+
+
+def load_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "of measured"}
+    return {"hbm_gbs": 6800.0, "source": "of fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.proc = None
+        self.lines: list[str] = []
+        self.dev = device_index
+
+    def start(self):
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(self.dev).uuid)
+            ident = ["--id=" + (uuid if uuid.startswith("GPU-") else "GPU-" + uuid)]
+        except Exception:
+            ident = []
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi"] + ident + ["--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def aggregate(per_rank_ms: list[float], units_per_rank: float, steps: int) -> tuple[float, float]:
+    """Whole-job throughput: the slowest rank's time bounds the job.  Returns
+    (units per second over all ranks, ms per step of the slowest rank)."""
+    ms = max(per_rank_ms)
+    return units_per_rank * len(per_rank_ms) * steps / (ms * steps / 1000.0), ms
+
+
+def cpu_baseline_sample(scale: int = 4) -> dict:
+    """The oracle's hash_cpu restatement on a 1/2^scale-size sample of every
+    variant (generation excluded, as the reference times it), one thread each."""
+    import numpy as np  # noqa: F401
+
+    from eating_one_gb300.workloads import workload
+    from oracle import oracle as O
+
+    rels = []
+    for v in VARIANTS:
+        w = workload(v, scale)
+        rels.append((O.generate(w["R"]), O.generate(w["S"])))
+    results = [None] * len(rels)
+
+    def one(i):
+        R, S = rels[i]
+        t0 = time.perf_counter()
+        rows = O.hash_join(R, S)
+        results[i] = (time.perf_counter() - t0, len(R) + len(S), len(rows))
+
+    threads = [threading.Thread(target=one, args=(i,)) for i in range(len(rels))]
+    t0 = time.perf_counter()
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    wall = time.perf_counter() - t0
+    tuples = sum(r[1] for r in results)
+    return {"value": tuples / wall, "unit": UNIT, "cores": len(rels), "kind": "port",
+            "sample": "oracle restatement of joins/CPU_JOIN/hash_cpu (partition by val %% 2^20 + bucket "
+                      "nested loop, rows materialised) on the three C3 variants at 1/%d size (R=2^%d, "
+                      "S=2^%d), one host thread per variant, generation excluded" % (2 ** scale, 26 - scale,
+                                                                                  28 - scale),
+            "seconds": round(wall, 3), "rows": sum(r[2] for r in results)}
+
+
+def run_reference(args) -> None:
+    """Reference arm: the reference CPU hash join (restated; the reference's own
+    binaries cannot be built where /root/reference is absent) on bounded samples."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    scale = 6
+    for _ in range(args.warmup):
+        cpu_baseline_sample(scale)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        r = cpu_baseline_sample(scale)
+        vals.append(r["value"])
+        secs.append(r["seconds"])
+    total_tuples = 3 * ((1 << (26 - scale)) + (1 << (28 - scale)))
+    value = total_tuples * len(secs) / sum(secs)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(secs) / len(secs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "config": {"workload": WORKLOAD + " (CPU sample at 1/64 size)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 3, "kind": "port",
+                             "sample": r["sample"].replace("1/16", "1/64")},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    from eating_one_gb300.build import build
+    from eating_one_gb300.engine import Engine
+    from eating_one_gb300.workloads import alg_bytes, workload
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if rank == 0:
+        build()
+    if dist:
+        dist.barrier()
+    eng = Engine(local)
+    peaks = load_peaks()
+
+    # inputs (weak scaling: every rank joins its own seeded relations)
+    joins = []
+    for v in VARIANTS:
+        w = workload(v)
+        for side in ("R", "S"):
+            w[side].seed ^= (rank * 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+        R, S = eng.generate(w["R"]), eng.generate(w["S"])
+        n_out = eng.count("hash", R, S)
+        out = torch.empty((n_out, 4), dtype=torch.int32, device="cuda")
+        joins.append({"name": v, "R": R, "S": S, "n_out": n_out, "out": out,
+                      "d_count": torch.zeros(1, dtype=torch.int64, device="cuda")})
+    units = sum(j["R"].shape[0] + j["S"].shape[0] for j in joins)
+
+    def step():
+        for j in joins:
+            eng.hash_join_async(j["R"], j["S"], j["out"], j["d_count"])
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert eng.sync_status() == 0, eng.last_error()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    eng.set_timing(True)
+    eng.phase_totals()
+    launches0 = eng.kernel_launches()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = eng.kernel_launches() - launches0
+    phases, njoins = eng.phase_totals()
+    eng.set_timing(False)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+
+    # every timed join must have produced exactly the counted rows, without device errors
+    status = eng.sync_status()
+    for j in joins:
+        assert int(j["d_count"].item()) == j["n_out"], (j["name"], int(j["d_count"].item()), j["n_out"])
+    assert status == 0, "device status %d: %s" % (status, eng.last_error())
+
+    per_rank = [ms]
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        g = [torch.zeros_like(t) for _ in range(world)]
+        dist.all_gather(g, t)
+        per_rank = [float(x.item()) for x in g]
+    value, ms_max = aggregate(per_rank, units, 1)
+
+    # roofline of the dominant phase (per join, averaged over the timed joins)
+    n_s = sum(j["S"].shape[0] for j in joins) / len(joins)
+    n_r = sum(j["R"].shape[0] for j in joins) / len(joins)
+    n_o = sum(j["n_out"] for j in joins) / len(joins)
+    names = ["build (R table: LSD radix passes + bucket starts)", "partition (S radix pass)",
+             "count (probe_count_kernel + scan)", "write (probe_write_kernel)"]
+    kernel = ["rx_scatter_kernel+rx_hist_kernel (R)", "rx_scatter_kernel+rx_hist_kernel (S)",
+              "probe_count_kernel", "probe_write_kernel"]
+    # algorithmic bytes per launch of each phase
+    phase_bytes = [24.0 * n_r * 3 + 4.0 * n_r, 24.0 * n_s, 8.0 * n_s, 8.0 * n_s + 16.0 * n_o]
+    per_join = [p / max(njoins, 1) for p in phases]
+    dom = max(range(4), key=lambda i: per_join[i])
+    achieved = phase_bytes[dom] / (per_join[dom] / 1000.0) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_c3.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get(kernel[dom])
+    alg = sum(alg_bytes("hash", j["R"].shape[0], j["S"].shape[0], j["n_out"]) for j in joins)
+    join_gbs = alg / (ms_max / 1000.0) / 1e9
+
+    # end to end through the host-buffer C ABI call
+    e2e = None
+    if args.e2e_steps > 0:
+        hosts = []
+        max_out = max(j["n_out"] for j in joins)
+        out_h = torch.empty((max_out, 4), dtype=torch.int32, pin_memory=True)
+        for j in joins:
+            hosts.append((j["R"].cpu().pin_memory(), j["S"].cpu().pin_memory(), j["n_out"]))
+        eng.join_host("hash", hosts[0][0], hosts[0][1], out_h)  # warm-up
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            for Rh, Sh, n_out in hosts:
+                n = eng.join_host("hash", Rh, Sh, out_h)
+                assert n == n_out
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        if dist:
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": units * world / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": int(sum(8 * (R.shape[0] + S.shape[0]) for R, S, _ in hosts)),
+               "d2h_bytes_per_step": int(sum(16 * n for _, _, n in hosts)),
+               "ms_per_step": round(e2e_s * 1000.0, 3)}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(4)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded device generators)",
+        "config": {"workload": WORKLOAD, "R": 1 << 26, "S": 1 << 28, "joins_per_step": len(joins),
+                   "results_per_step": int(sum(j["n_out"] for j in joins)),
+                   "l2": "inputs larger than L2 (R 512 MB, S 2 GB per join)", "parallelism": "dp%d" % world},
+        "roofline": {"bound": "hbm", "kernel": kernel[dom], "phase": names[dom],
+                     "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+                     "peak_source": peaks["source"],
+                     "bytes_per_launch": int(phase_bytes[dom]), "ms_per_launch": round(per_join[dom], 4)},
+        "join_roofline": {"alg_bytes_per_step": int(alg), "achieved": round(join_gbs, 1), "unit": "GB/s",
+                          "frac": round(join_gbs / peaks["hbm_gbs"], 4), "peak_source": peaks["source"]},
+        "phases_ms_per_join": {"build": round(per_join[0], 4), "partition": round(per_join[1], 4),
+                               "count": round(per_join[2], 4), "write": round(per_join[3], 4)},
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -27,6 +27,7 @@ ej_status ej_fail(ej_handle* h, ej_status s, const char* fmt, ...) {
 ej_status ej_check_launch(ej_handle* h, const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return ej_fail(h, EJ_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+  h->launches++;
   return EJ_OK;
 }
 
@@ -74,7 +75,6 @@ extern "C" ej_status ej_create(int device, ej_handle** out) {
             cudaMalloc(&h->d_words, 8 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaMallocHost(&h->h_words, 8 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaMallocHost(&h->h_status, sizeof(ej_dev_status)) == cudaSuccess;
-  for (int i = 0; ok && i < 4; i++) ok = cudaEventCreate(&h->ev[i]) == cudaSuccess;
   if (ok) ok = cudaMemset(h->d_status, 0, sizeof(ej_dev_status)) == cudaSuccess &&
                cudaMemset(h->d_words, 0, 8 * sizeof(unsigned long long)) == cudaSuccess;
   if (!ok) {
@@ -97,8 +97,7 @@ extern "C" ej_status ej_destroy(ej_handle* h) {
   cudaFree(h->zipf.d_cdf);
   cudaFreeHost(h->h_words);
   cudaFreeHost(h->h_status);
-  for (int i = 0; i < 4; i++)
-    if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+  for (cudaEvent_t e : h->ring) cudaEventDestroy(e);
   delete h;
   return EJ_OK;
 }
@@ -124,7 +123,41 @@ extern "C" ej_status ej_trim(ej_handle* h) {
 
 extern "C" ej_status ej_set_timing(ej_handle* h, int enable) {
   if (!h) return EJ_ERR_INVALID;
+  if (enable && h->ring.empty()) {
+    EJ_CUDA(h, cudaSetDevice(h->device));
+    h->ring.resize((size_t)EJ_PHASE_RING * (EJ_PHASES + 1), nullptr);
+    for (cudaEvent_t& e : h->ring) EJ_CUDA(h, cudaEventCreate(&e));
+  }
   h->timing = enable != 0;
+  return EJ_OK;
+}
+
+extern "C" uint64_t ej_kernel_launches(const ej_handle* h) { return h ? (uint64_t)h->launches : 0; }
+
+void ej_phase_begin(ej_handle* h) {
+  if (!h->timing || h->ring.empty()) {
+    h->cur_set = -1;
+    return;
+  }
+  h->cur_set = (int)h->ring_head;
+  h->ring_head = (h->ring_head + 1) % EJ_PHASE_RING;
+  cudaEventRecord(h->ring[(size_t)h->cur_set * (EJ_PHASES + 1)], h->stream);
+}
+
+void ej_phase_mark(ej_handle* h, int k) {
+  if (h->cur_set < 0) return;
+  cudaEventRecord(h->ring[(size_t)h->cur_set * (EJ_PHASES + 1) + k], h->stream);
+  if (k == EJ_PHASES) {
+    h->last_set = h->cur_set;
+    h->cur_set = -1;
+    if (h->ring_pending < EJ_PHASE_RING) h->ring_pending++;
+  }
+}
+
+static ej_status set_phases(ej_handle* h, int set, float ms[EJ_PHASES]) {
+  cudaEvent_t* e = &h->ring[(size_t)set * (EJ_PHASES + 1)];
+  EJ_CUDA(h, cudaEventSynchronize(e[EJ_PHASES]));
+  for (int i = 0; i < EJ_PHASES; i++) EJ_CUDA(h, cudaEventElapsedTime(&ms[i], e[i], e[i + 1]));
   return EJ_OK;
 }
 
@@ -143,9 +176,25 @@ extern "C" ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value) {
   return ej_fail(h, EJ_ERR_INVALID, "unknown option %d", (int)opt);
 }
 
-extern "C" ej_status ej_last_phase_ms(const ej_handle* h, float ms[3]) {
+extern "C" ej_status ej_last_phase_ms(ej_handle* h, float ms[EJ_PHASES]) {
   if (!h || !ms) return EJ_ERR_INVALID;
-  for (int i = 0; i < 3; i++) ms[i] = h->phase_ms[i];
+  for (int i = 0; i < EJ_PHASES; i++) ms[i] = 0.f;
+  if (h->last_set < 0) return EJ_OK;
+  return set_phases(h, h->last_set, ms);
+}
+
+extern "C" ej_status ej_phase_totals(ej_handle* h, double ms[EJ_PHASES], uint32_t* joins) {
+  if (!h || !ms) return EJ_ERR_INVALID;
+  for (int i = 0; i < EJ_PHASES; i++) ms[i] = 0.0;
+  const uint32_t n = h->ring_pending;
+  for (uint32_t j = 0; j < n; j++) {
+    const int set = (int)((h->ring_head + EJ_PHASE_RING - 1 - (h->cur_set >= 0 ? 1 : 0) - j) % EJ_PHASE_RING);
+    float f[EJ_PHASES];
+    EJ_TRY(set_phases(h, set, f));
+    for (int i = 0; i < EJ_PHASES; i++) ms[i] += f[i];
+  }
+  h->ring_pending = 0;
+  if (joins) *joins = n;
   return EJ_OK;
 }
 
@@ -180,11 +229,6 @@ ej_status ej_finish(ej_handle* h, uint64_t* count) {
   EJ_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(ej_dev_status), h->stream));
   EJ_CUDA(h, cudaStreamSynchronize(h->stream));
   if (count) *count = h->h_words[0];
-  if (h->timed_pending) {
-    for (int i = 0; i < 3; i++) cudaEventElapsedTime(&h->phase_ms[i], h->ev[i], h->ev[i + 1]);
-    cudaGetLastError();
-    h->timed_pending = false;
-  }
   const unsigned int code = h->h_status->code;
   if (code != 0 && code != EJ_ERR_CAPACITY)
     return ej_fail(h, (ej_status)code, "device reported %s (site %u)", ej_status_name((ej_status)code),

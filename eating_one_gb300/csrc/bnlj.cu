@@ -231,9 +231,9 @@ static ej_status bnl_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_
   splits = (nS + s_per_cta - 1) / s_per_cta;
   const dim3 grid((unsigned)rchunks, (unsigned)splits);
   const bool tma = ((uintptr_t)S % 16) == 0;
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+  // one pass: the whole nested loop is recorded as the write phase
+  ej_phase_begin(h);
+  for (int k = 1; k < EJ_PHASES; k++) ej_phase_mark(h, k);
   ej_status st;
   if (count_only)
     st = tma ? launch_bnl<true, true>(h, grid, R, nR, S, nS, s_per_cta, out, cap)
@@ -241,10 +241,7 @@ static ej_status bnl_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_
   else
     st = tma ? launch_bnl<true, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap)
              : launch_bnl<false, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap);
-  if (h->timing && st == EJ_OK) {
-    EJ_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
-    h->timed_pending = true;
-  }
+  ej_phase_mark(h, EJ_PHASES);
   return st;
 }
 

@@ -5,6 +5,7 @@
 #include <stdarg.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 #include "ej.h"
 
@@ -36,11 +37,14 @@ struct ej_handle {
   unsigned long long* h_words = nullptr;  // pinned host mirror
   ej_dev_status* h_status = nullptr;      // pinned host mirror of d_status
   std::string last_error;
-  // phase timing
+  // phase timing: a ring of EJ_PHASE_RING sets of EJ_PHASES+1 events
   bool timing = false;
-  bool timed_pending = false;  // ev[0..3] recorded by the current call
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  float phase_ms[3] = {0.f, 0.f, 0.f};
+  std::vector<cudaEvent_t> ring;
+  uint32_t ring_head = 0;     // next set to record
+  uint32_t ring_pending = 0;  // recorded sets not yet summed by ej_phase_totals
+  int cur_set = -1;           // set of the join being recorded, -1 when none
+  int last_set = -1;          // last fully recorded set
+  unsigned long long launches = 0;  // kernels launched through ej_check_launch
   ej_zipf_cache zipf;
   // tuning overrides (-1 / 0 = planner's choice)
   int opt_partition_bits = -1;
@@ -64,6 +68,10 @@ ej_status ej_fail(ej_handle* h, ej_status s, const char* fmt, ...);
 ej_status ej_arena_reserve(ej_handle* h, size_t bytes);
 inline char* ej_arena_at(ej_handle* h, size_t off) { return static_cast<char*>(h->arena) + off; }
 ej_status ej_check_launch(ej_handle* h, const char* what);
+// phase timing: begin a join's event set (mark 0), then marks 1..EJ_PHASES at
+// the phase boundaries (build | partition | count | write); no-ops when timing is off
+void ej_phase_begin(ej_handle* h);
+void ej_phase_mark(ej_handle* h, int k);
 ej_status ej_read_count(ej_handle* h, uint64_t* out_count);  // sync + read d_words[0]
 ej_status ej_take_status(ej_handle* h);                      // sync + read/clear d_status
 

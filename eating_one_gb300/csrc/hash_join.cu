@@ -372,7 +372,8 @@ void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint
   ej_probe_plan(p, L.pp, nS);
 }
 
-// Partition S (when the layout says so), count, scan and write.  The arena
+// Partition S (when the layout says so), count, scan and write; records
+// phase marks 2..4 (the caller has begun the set and marked the build).  The arena
 // must already hold the layout (reserved together with anything the table
 // placed there, so that no reservation moves a built table).
 ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_view& t, const ej_tuple* S,
@@ -384,14 +385,11 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
     EJ_TRY(ej_radix_pass(h, L.splan, S, spart, 32u - L.pb, L.pb));
     P = spart;
   }
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+  ej_phase_mark(h, 2);
   EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+  ej_phase_mark(h, 3);
   if (!count_only) EJ_TRY(ej_probe_write(h, L.pp, P, t, outer, out, out_cap));
-  if (h->timing) {
-    EJ_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
-    h->timed_pending = true;
-  }
+  ej_phase_mark(h, 4);
   return EJ_OK;
 }
 
@@ -405,9 +403,10 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   ej_probe_layout L;
   ej_probe_layout_add(p, L, nS, pb);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  ej_phase_begin(h);
   ej_tuple* rs = reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.rs_off));
   ej_table_view t;
   EJ_TRY(ej_table_build(h, tp, R, rs, ej_arena_at(h, tp.start_off), &t));
+  ej_phase_mark(h, 1);
   return ej_probe_exec(h, L, t, S, /*outer=*/false, mode == 2, out, out_cap, d_count);
 }

@@ -48,7 +48,9 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
     delete ix;
     return ej_fail(h, EJ_ERR_NOMEM, "index storage of %zu bytes could not be allocated", rs_bytes + aux_bytes);
   }
+  ej_phase_begin(h);
   ej_status st = ej_table_build(h, tp, R, ix->rs, ix->aux, &ix->view);
+  for (int k = 1; k <= EJ_PHASES; k++) ej_phase_mark(h, k);
   if (st == EJ_OK) st = ej_finish(h, nullptr);
   if (st != EJ_OK) {
     cudaFree(ix->rs);
@@ -98,7 +100,8 @@ static ej_status index_probe(ej_handle* h, const ej_index* ix, const ej_tuple* S
   ej_probe_layout L;
   ej_probe_layout_add(p, L, nS, pb);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  ej_phase_begin(h);
+  ej_phase_mark(h, 1);
   EJ_TRY(ej_probe_exec(h, L, ix->view, S, outer, count_only, out, cap, h->d_words));
   uint64_t count = 0;
   EJ_TRY(ej_finish(h, &count));
@@ -157,10 +160,11 @@ extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_
   ej_probe_layout L;
   ej_probe_layout_add(p, L, nS, pb);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  ej_phase_begin(h);
   ej_table_view t;
   EJ_TRY(ej_table_build(h, tp, R, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.rs_off)),
                         ej_arena_at(h, tp.start_off), &t));
+  ej_phase_mark(h, 1);
   EJ_TRY(ej_probe_exec(h, L, t, S, /*outer=*/true, false, out, out_cap, h->d_words));
   uint64_t count = 0;
   EJ_TRY(ej_finish(h, &count));
@@ -278,13 +282,14 @@ extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tu
   const size_t off_off = p.add((ntiles + 1) * sizeof(unsigned long long));
   const size_t scan_off = p.add(ej_scan_scratch_bytes(ntiles));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
+  ej_phase_begin(h);
   ej_table_view t1, t2;
   EJ_TRY(ej_table_build(h, tp1, D1, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp1.rs_off)),
                         ej_arena_at(h, tp1.start_off), &t1));
   EJ_TRY(ej_table_build(h, tp2, D2, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp2.rs_off)),
                         ej_arena_at(h, tp2.start_off), &t2));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+  ej_phase_mark(h, 1);
+  ej_phase_mark(h, 2);
   unsigned long long* tcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, count_off));
   unsigned long long* toff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, off_off));
   if (ntiles) {
@@ -294,16 +299,13 @@ extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tu
   EJ_TRY(ej_scan_u64_u64(h, tcount, ntiles, toff, ej_arena_at(h, scan_off)));
   EJ_CUDA(h, cudaMemcpyAsync(h->d_words, toff + ntiles, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
                              h->stream));
-  if (h->timing) EJ_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+  ej_phase_mark(h, 3);
   if (ntiles) {
     star_write_kernel<<<(unsigned)ntiles, ST_THREADS, 0, h->stream>>>(F1, F2, nF, t1, t2, toff, ntiles, out, out_cap,
                                                                      h->d_status);
     EJ_TRY(ej_check_launch(h, "star_write_kernel"));
   }
-  if (h->timing) {
-    EJ_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
-    h->timed_pending = true;
-  }
+  ej_phase_mark(h, 4);
   uint64_t count = 0;
   EJ_TRY(ej_finish(h, &count));
   *out_count = count;

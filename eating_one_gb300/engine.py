@@ -100,9 +100,20 @@ class Engine:
         self._check(self.lib.ej_set_timing(self.h, 1 if enable else 0))
 
     def phase_ms(self) -> list[float]:
-        arr = (C.c_float * 3)()
+        """Device time of the last timed join's phases: build, partition, count, write (ms)."""
+        arr = (C.c_float * native.EJ_PHASES)()
         self._check(self.lib.ej_last_phase_ms(self.h, arr))
         return list(arr)
+
+    def phase_totals(self) -> tuple[list[float], int]:
+        """Summed phase times of every join timed since the last call, and how many joins."""
+        arr = (C.c_double * native.EJ_PHASES)()
+        n = C.c_uint32(0)
+        self._check(self.lib.ej_phase_totals(self.h, arr, C.byref(n)))
+        return list(arr), n.value
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.ej_kernel_launches(self.h))
 
     def scratch_bytes(self) -> int:
         return int(self.lib.ej_scratch_bytes(self.h))

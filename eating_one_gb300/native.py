@@ -59,6 +59,8 @@ _SIGS = {
     "ej_trim": [_vp],
     "ej_set_timing": [_vp, _i32],
     "ej_last_phase_ms": [_vp, C.POINTER(C.c_float)],
+    "ej_phase_totals": [_vp, C.POINTER(C.c_double), C.POINTER(C.c_uint32)],
+    "ej_kernel_launches": [_vp],
     "ej_set_option": [_vp, _i32, C.c_int64],
     "ej_hash_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_hash_join_count": [_vp, _vp, _u64, _vp, _u64, _pu64],
@@ -83,7 +85,9 @@ _SIGS = {
     "ej_generate": [_vp, C.POINTER(GenSpec), _vp],
     "ej_checksum": [_vp, _vp, _u64, C.c_uint32, _pu64],
 }
-_RESTYPES = {"ej_status_name": C.c_char_p, "ej_last_error": C.c_char_p, "ej_scratch_bytes": C.c_uint64}
+_RESTYPES = {"ej_status_name": C.c_char_p, "ej_last_error": C.c_char_p, "ej_scratch_bytes": C.c_uint64,
+             "ej_kernel_launches": C.c_uint64}
+EJ_PHASES = 4  # build | partition | count | write
 
 _lib = None
 

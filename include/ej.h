@@ -92,11 +92,19 @@ const char* ej_last_error(const ej_handle* h);
 uint64_t ej_scratch_bytes(const ej_handle* h);
 /* release the handle's cached scratch (the next call re-allocates) */
 ej_status ej_trim(ej_handle* h);
-/* device time of the last join's phases, milliseconds: [0] partition/build,
- * [1] count + scan, [2] write; like the reference's phase timers
- * (hj.cc:1194-1237), measured with CUDA events when timing is enabled */
+/* Phase timers, like the reference's (hj.cc:1194-1237) but measured on the
+ * device with CUDA events when timing is enabled.  Phases of one join, in
+ * milliseconds: [0] build (R table / index), [1] partition (S radix pass),
+ * [2] count + scan, [3] write.  Joins run while timing is on record into a
+ * ring of EJ_PHASE_RING event sets; ej_phase_totals synchronises, sums every
+ * set recorded since the previous call and clears the ring. */
+#define EJ_PHASES 4
+#define EJ_PHASE_RING 512
 ej_status ej_set_timing(ej_handle* h, int enable);
-ej_status ej_last_phase_ms(const ej_handle* h, float ms[3]);
+ej_status ej_last_phase_ms(ej_handle* h, float ms[EJ_PHASES]);
+ej_status ej_phase_totals(ej_handle* h, double ms[EJ_PHASES], uint32_t* joins);
+/* number of CUDA kernels this handle has launched (all entry points) */
+uint64_t ej_kernel_launches(const ej_handle* h);
 
 /* Tuning knobs (the reference's compile-time #defines, e.g. PARTITION/RADIX/
  * PART_STANDARD in joins/hashJoin_gpu/main_street/tuple.h:1-16, become runtime
