@@ -89,8 +89,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     # the reference-style command-line driver, linked against the library
     cli_src = os.path.join(PKG_DIR, "cli", "ej_join.cpp")
     if os.path.exists(cli_src):
-        _run(["g++", "-O2", "-std=c++17", "-I", INCLUDE, cli_src, "-o", CLI_PATH + ".tmp",
-              "-L", PKG_DIR, "-leating_one", "-Wl,-rpath,$ORIGIN"])
+        _run([nvcc, "-O2", "-std=c++17", "-I", INCLUDE, cli_src, "-o", CLI_PATH + ".tmp",
+              "-L", PKG_DIR, "-leating_one", "-Xlinker", "-rpath,$ORIGIN"])
         os.replace(CLI_PATH + ".tmp", CLI_PATH)
     return LIB_PATH
 
