@@ -6,6 +6,8 @@
 // replaces its input buffer.  Here: one launch, inputs untouched, n+1 outputs
 // (the last one is the total, so no separate getValue readback kernel,
 // scan_main.cpp:160-180), 64-bit outputs where totals can exceed 2^32.
+#include <mutex>
+
 #include "ej_device.cuh"
 
 namespace {
@@ -106,4 +108,90 @@ ej_status ej_scan_u32_u64(ej_handle* h, const uint32_t* in, uint64_t n, unsigned
 ej_status ej_scan_u64_u64(ej_handle* h, const unsigned long long* in, uint64_t n,
                           unsigned long long* out, void* scratch) {
   return launch_scan<unsigned long long, unsigned long long>(h, in, n, out, scratch);
+}
+
+// ---- scan without allocation ------------------------------------------------
+// For callers that cannot allocate device memory (their framework owns the
+// GPU's memory, they must not trigger the device-wide synchronisation of
+// cudaMalloc/cudaFree, or they cannot keep a handle).  The look-back scratch
+// is this file-scope array instead of handle memory; every device that loads
+// the library holds it until the process exits.
+
+namespace {
+
+constexpr uint64_t NOALLOC_TILES = (EJ_NOALLOC_SCAN_MAX_N + SCAN_TILE - 1) / SCAN_TILE;  // 65536
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+// look-back status words of every tile, then one word holding the tile counter
+static __device__ __align__(256) unsigned long long g_noalloc_scan_scratch[NOALLOC_TILES + 1];
+// device status word of the no-allocation scan (bounded-wait timeouts)
+static __device__ __align__(256) ej_dev_status g_noalloc_scan_status;
+
+struct NoallocDevice {
+  bool ready = false;
+  unsigned long long* scratch = nullptr;  // device address of g_noalloc_scan_scratch
+  ej_dev_status* status = nullptr;        // device address of g_noalloc_scan_status
+};
+NoallocDevice g_noalloc_devices[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_mutex;
+
+}  // namespace
+
+extern "C" ej_status ej_exclusive_scan_u32_noalloc(const uint32_t* in, uint64_t n, uint64_t* out,
+                                                   ej_stream stream) {
+  if ((n && !in) || !out) return EJ_ERR_INVALID;
+  if (n > EJ_NOALLOC_SCAN_MAX_N) return EJ_ERR_TOO_LARGE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return EJ_ERR_NO_DEVICE;
+  }
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return EJ_ERR_INVALID;
+  NoallocDevice& d = g_noalloc_devices[dev];
+  {
+    // set-up once per device, with that device current: the host-side names of
+    // the static arrays are not device addresses, so look the addresses up
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!d.ready) {
+      void* scratch = nullptr;
+      void* status = nullptr;
+      if (cudaGetSymbolAddress(&scratch, g_noalloc_scan_scratch) != cudaSuccess ||
+          cudaGetSymbolAddress(&status, g_noalloc_scan_status) != cudaSuccess) {
+        cudaGetLastError();
+        return EJ_ERR_CUDA;
+      }
+      d.scratch = static_cast<unsigned long long*>(scratch);
+      d.status = static_cast<ej_dev_status*>(status);
+      d.ready = true;
+    }
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
+  if (n == 0) {
+    if (cudaMemsetAsync(o, 0, sizeof(unsigned long long), s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      cudaGetLastError();
+      return EJ_ERR_CUDA;
+    }
+    return EJ_OK;
+  }
+  const uint64_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  // the array keeps the previous call's words: clear the status words, the
+  // tile counter and the status word before every launch
+  if (cudaMemsetAsync(d.scratch, 0, (ntiles + 1) * sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(d.status, 0, sizeof(ej_dev_status), s) != cudaSuccess) {
+    cudaGetLastError();
+    return EJ_ERR_CUDA;
+  }
+  unsigned int* ctr = reinterpret_cast<unsigned int*>(d.scratch + ntiles);
+  scan_kernel<uint32_t, unsigned long long><<<(unsigned)ntiles, SCAN_THREADS, 0, s>>>(in, n, o, d.scratch, ctr,
+                                                                                     ntiles, d.status);
+  if (cudaGetLastError() != cudaSuccess) return EJ_ERR_CUDA;
+  ej_dev_status host_status;
+  if (cudaMemcpyAsync(&host_status, d.status, sizeof(host_status), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaGetLastError();
+    return EJ_ERR_CUDA;
+  }
+  return host_status.code ? (ej_status)host_status.code : EJ_OK;
 }

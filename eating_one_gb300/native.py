@@ -82,6 +82,7 @@ _SIGS = {
     "ej_join": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_join_host": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_exclusive_scan_u32": [_vp, _vp, _u64, _vp],
+    "ej_exclusive_scan_u32_noalloc": [_vp, _u64, _vp, _vp],
     "ej_generate": [_vp, C.POINTER(GenSpec), _vp],
     "ej_checksum": [_vp, _vp, _u64, C.c_uint32, _pu64],
 }

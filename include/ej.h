@@ -211,6 +211,24 @@ ej_status ej_join_host(ej_handle* h, ej_algo algo, const ej_tuple* R, uint64_t n
  * in place, pads to 2048/2^20 multiples and frees its input. */
 ej_status ej_exclusive_scan_u32(ej_handle* h, const uint32_t* in, uint64_t n, uint64_t* out);
 
+/* The same scan for callers that cannot allocate device memory: code whose
+ * host framework already owns all of the GPU's memory through its own pool,
+ * code that must not call cudaMalloc/cudaFree because they synchronise the
+ * whole device, and code that cannot keep an ej_handle (creating one
+ * allocates).  No counterpart in the reference.  It allocates nothing: its
+ * look-back scratch is a static device array sized for at most
+ * EJ_NOALLOC_SCAN_MAX_N inputs (about 512 KB, held on every device that loads
+ * the library until the process exits); larger n returns EJ_ERR_TOO_LARGE.
+ * in and out (n + 1 uint64 offsets, out[n] = total) are device pointers owned
+ * by the caller; the scan runs on `stream` on the current device and the call
+ * returns after it has finished.  The first call on a device looks up the
+ * scratch address for that device; make that first call before any stream
+ * capture.  All calls share the one scratch array, so calls that overlap on
+ * the GPU (other streams or host threads) race and must be serialised by the
+ * caller. */
+#define EJ_NOALLOC_SCAN_MAX_N (1ull << 28)
+ej_status ej_exclusive_scan_u32_noalloc(const uint32_t* in, uint64_t n, uint64_t* out, ej_stream stream);
+
 /* ---- inputs and checks --------------------------------------------------- */
 
 /* Fill a device relation from a generator spec (see ej_gen.h).  For Zipf specs
