@@ -119,17 +119,24 @@ uint32_t ej_radix_tiles(uint64_t n);
 void ej_radix_plan_add(ej_plan_bytes& p, ej_radix_plan& rp, uint64_t n);
 ej_status ej_radix_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
                         uint32_t shift, uint32_t bits, int digit_kind = EJ_DIGIT_HASH);
+// the same pass writing keys and vals to two arrays (last pass of a table build)
+ej_status ej_radix_pass_soa(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, int32_t* out_keys,
+                            int32_t* out_vals, uint32_t shift, uint32_t bits, int digit_kind);
 
 // ---- probe targets (hash_join.cu) -----------------------------------------
-// EJ_TABLE_HASH: R sorted by bucket id (top `hb` bits of hash32(val)) plus
-//   bucket starts; a probe scans its bucket and compares val.
-// EJ_TABLE_SORTED: R sorted by val; a probe binary-searches the matching run,
-//   narrowed first by a fence of every 256th val.
+// R is stored as two arrays, rkey[] and rval[], in one order:
+// EJ_TABLE_HASH: sorted by hash32(val), so equal keys form one contiguous run
+//   and bucket b (top `hb` hash bits) is [start[b], start[b+1]).
+// EJ_TABLE_SORTED: sorted by val; the run of a value is found by binary
+//   search, narrowed first by a fence of every 256th val.
+// Both arrays carry EJ_TABLE_PAD readable elements past nR (vector loads).
 enum { EJ_TABLE_HASH = 0, EJ_TABLE_SORTED = 1 };
 constexpr uint32_t EJ_FENCE_STRIDE = 256;
+constexpr uint64_t EJ_TABLE_PAD = 8;
 struct ej_table_view {
   int kind = EJ_TABLE_HASH;
-  const ej_tuple* rs = nullptr;      // R in bucket (or val) order
+  const int32_t* rkey = nullptr;     // [nR + pad] row ids in table order
+  const int32_t* rval = nullptr;     // [nR + pad] join keys in table order (16-byte aligned)
   const uint32_t* start = nullptr;   // [2^hb + 1] (hash)
   const int32_t* fence = nullptr;    // [nfence] (sorted)
   uint64_t nR = 0;

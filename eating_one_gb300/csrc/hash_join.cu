@@ -1,4 +1,5 @@
-// hash_join.cu - bucketised hash table on R and the count -> scan -> write probe.
+// hash_join.cu - the table build and the probe (count, and write with
+// decoupled look-back) shared by every join that probes R.
 //
 // Reference path replaced (joins/hashJoin_gpu/main_street): radix-partition
 // both relations into ~|R|/64 partitions, split left partitions into 256-tuple
@@ -7,106 +8,58 @@
 // compares per block, and the write pass repeats all of them.
 //
 // Here:
-//   build  R is sorted stably by bucket id = top `hb` bits of hash32(val)
-//          (LSD radix passes, radix.cu), and start[b] marks where bucket b
-//          begins - the layout of the reference's hash index (Bucket grouped by
-//          bucket + Buck_array offsets, joins/CPU_JOIN/inner_cpu/
-//          inner-idx-bnlj.cc:142-166), built on the device.
+//   build  R is sorted by hash32(val) with four 8-bit LSD radix passes
+//          (radix.cu); the last pass writes it as two arrays rkey[]/rval[],
+//          and start[b] marks where bucket b (top hb hash bits) begins - the
+//          grouped layout of the reference's hash index (Bucket + Buck_array,
+//          joins/CPU_JOIN/inner_cpu/inner-idx-bnlj.cc:142-166), built on the
+//          device.  The hash is a bijection, so equal keys are one contiguous
+//          run and a probe yields (run start, run length).
 //   S      when the table does not fit in L2, S is radix-partitioned once by
-//          the top `pb` hash bits, so probes of consecutive tiles touch one
-//          table region at a time and hit L2; otherwise S is probed in place.
-//   probe  count kernel (matches per 2048-tuple tile) -> look-back scan of the
-//          tile counts (64-bit) -> write kernel (block scan of per-thread
-//          counts, rows written at tile offset + thread prefix).  Output order
-//          is deterministic: tile, thread, item, then R order.
-// The same probe kernels serve the sort index (ej_table_view kind
-// EJ_TABLE_SORTED: the matching run is found by binary search) and the left
-// outer join (OUTER: an unmatched probe row yields one NULL-extended row).
+//          the top pb hash bits, so consecutive probe tiles touch one table
+//          region at a time and hit L2; otherwise S is probed in place.
+//   write  one kernel per join: each 1024-probe tile finds its runs, scans
+//          its counts, takes its output offset from the preceding tiles by
+//          decoupled look-back (tiles claim ids in order), then expands the
+//          runs into rows staged in shared memory and written out as
+//          coalesced 16-byte streaming stores.  Probes with many matches are
+//          expanded by the whole block.  The separate count kernel + scan
+//          serve the *_count entry points.  Output order is deterministic:
+//          tile, probe, then R run order.
+// The same kernels serve the sort index (runs by binary search) and the left
+// outer join (OUTER: a probe without matches yields one NULL-extended row).
 #include "ej_device.cuh"
 #include "hash_join.cuh"
+#include "probe.cuh"
 
 namespace {
 
 constexpr int PR_THREADS = 256;
-constexpr int PR_ITEMS = 8;
-constexpr int PR_TILE = PR_THREADS * PR_ITEMS;
+constexpr int PR_ITEMS = 4;
+constexpr int PR_TILE = PR_THREADS * PR_ITEMS;  // 1024 probes
+constexpr int PW_STAGE = 2048;                  // staged output rows per chunk (32 KB)
+constexpr uint32_t PW_LIGHT = 8;                // more matches: expanded by the whole block
+constexpr uint32_t NULL_RUN = 0xFFFFFFFFu;      // OUTER: the NULL-extended row
 
-__device__ __forceinline__ uint32_t bucket_of(int32_t val, uint32_t bshift) {
-  return ej_hash32((uint32_t)val) >> bshift;
-}
-
-// start[b] = first position of bucket b in the bucket-sorted relation, b in [0, 2^hb].
-__global__ void bucket_start_kernel(const ej_tuple* __restrict__ rs, uint64_t nR, uint32_t* __restrict__ start,
+// start[b] = first position of bucket b in the hash-sorted table, b in [0, 2^hb].
+__global__ void bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint32_t* __restrict__ start,
                                     uint32_t hb) {
-  const uint32_t bshift = 32u - hb;
   const int64_t nbuckets = (int64_t)1 << hb;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nR;
        i += (uint64_t)gridDim.x * blockDim.x) {
-    const int64_t cur = i < nR ? (int64_t)bucket_of(rs[i].val, bshift) : nbuckets;
-    const int64_t prev = i > 0 ? (int64_t)bucket_of(rs[i - 1].val, bshift) : -1;
+    const int64_t cur = i < nR ? (int64_t)ej_bucket_of(rval[i], hb) : nbuckets;
+    const int64_t prev = i > 0 ? (int64_t)ej_bucket_of(rval[i - 1], hb) : -1;
     for (int64_t b = prev + 1; b <= cur; b++) start[b] = (uint32_t)i;
   }
 }
 
-// fence[i] = rs[i * EJ_FENCE_STRIDE].val of a val-sorted relation
-__global__ void fence_kernel(const ej_tuple* __restrict__ rs, uint64_t nR, int32_t* __restrict__ fence,
-                             uint32_t nfence) {
+// fence[i] = rval[i * EJ_FENCE_STRIDE] of a val-sorted table
+__global__ void fence_kernel(const int32_t* __restrict__ rval, int32_t* __restrict__ fence, uint32_t nfence) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nfence; i += gridDim.x * blockDim.x)
-    fence[i] = rs[(uint64_t)i * EJ_FENCE_STRIDE].val;
+    fence[i] = rval[(uint64_t)i * EJ_FENCE_STRIDE];
 }
 
-// ---- where a probe value's candidates lie ------------------------------------
-
-template <int KIND>
-struct Range;
-
-template <>
-struct Range<EJ_TABLE_HASH> {
-  // candidates: the whole bucket; callers compare val
-  static __device__ __forceinline__ void find(const ej_table_view& t, int32_t v, uint32_t& lo, uint32_t& hi) {
-    const uint32_t b = bucket_of(v, 32u - t.hb);
-    lo = __ldg(t.start + b);
-    hi = __ldg(t.start + b + 1);
-  }
-};
-
-// first index in [lo, hi) of the val-sorted relation whose val is >= v
-// (STRICT: > v), hi when there is none
-template <bool STRICT>
-__device__ __forceinline__ uint32_t sorted_bound(const int* vals2, uint32_t lo, uint32_t hi, int32_t v) {
-  while (lo < hi) {
-    const uint32_t mid = lo + ((hi - lo) >> 1);
-    const int32_t x = __ldg(vals2 + 2 * (uint64_t)mid);
-    if (STRICT ? (x <= v) : (x < v)) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
-template <bool STRICT>
-__device__ __forceinline__ uint32_t fenced_bound(const ej_table_view& t, int32_t v) {
-  // fence search: first fence entry f with fence[f] >= v (STRICT: > v)
-  uint32_t flo = 0, fhi = t.nfence;
-  while (flo < fhi) {
-    const uint32_t mid = (flo + fhi) >> 1;
-    const int32_t x = __ldg(t.fence + mid);
-    if (STRICT ? (x <= v) : (x < v)) flo = mid + 1; else fhi = mid;
-  }
-  if (flo == 0) return 0;
-  const uint64_t seg_lo = (uint64_t)(flo - 1) * EJ_FENCE_STRIDE;
-  const uint64_t seg_hi = min((uint64_t)flo * EJ_FENCE_STRIDE, t.nR);
-  return sorted_bound<STRICT>(reinterpret_cast<const int*>(t.rs) + 1, (uint32_t)seg_lo, (uint32_t)seg_hi, v);
-}
-
-template <>
-struct Range<EJ_TABLE_SORTED> {
-  // candidates: exactly the run of equal vals
-  static __device__ __forceinline__ void find(const ej_table_view& t, int32_t v, uint32_t& lo, uint32_t& hi) {
-    lo = fenced_bound<false>(t, v);
-    hi = fenced_bound<true>(t, v);
-  }
-};
-
-// ---- count and write kernels ------------------------------------------------------
+// ---- count (for the *_count entry points) ---------------------------------------
 
 template <int KIND, bool OUTER>
 __global__ void __launch_bounds__(PR_THREADS)
@@ -115,32 +68,20 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   __shared__ unsigned long long warp_tmp[PR_THREADS / 32 + 1];
   const uint64_t base = (uint64_t)blockIdx.x * PR_TILE;
   const int* pv = reinterpret_cast<const int*>(P) + 1;
-  const int* rv = reinterpret_cast<const int*>(t.rs) + 1;
   int v[PR_ITEMS];
-  uint32_t lo[PR_ITEMS], hi[PR_ITEMS];
 #pragma unroll
   for (int j = 0; j < PR_ITEMS; j++) {
     const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
     v[j] = idx < nP ? __ldcs(pv + 2 * idx) : 0;
   }
-#pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    lo[j] = hi[j] = 0;
-    if (idx < nP) Range<KIND>::find(t, v[j], lo[j], hi[j]);
-  }
   unsigned long long c = 0;
 #pragma unroll
   for (int j = 0; j < PR_ITEMS; j++) {
     const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    uint32_t m;
-    if (KIND == EJ_TABLE_SORTED) {
-      m = hi[j] - lo[j];
-    } else {
-      m = 0;
-      for (uint32_t i = lo[j]; i < hi[j]; i++) m += (__ldg(rv + 2 * (uint64_t)i) == v[j]);
-    }
-    if (OUTER && idx < nP && m == 0) m = 1;
+    if (idx >= nP) continue;
+    uint32_t lo, m;
+    EjRun<KIND>::find(t, v[j], lo, m);
+    if (OUTER && m == 0) m = 1;
     c += m;
   }
   unsigned long long total;
@@ -148,67 +89,125 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   if (threadIdx.x == 0) tile_count[blockIdx.x] = total;
 }
 
-__device__ __forceinline__ void store_row(ej_result* out, uint64_t pos, int32_t rk, int32_t rv, int32_t lk,
-                                          int32_t lv) {
-  __stcs(reinterpret_cast<int4*>(out + pos), make_int4(rk, rv, lk, lv));
+// ---- write with decoupled look-back ---------------------------------------------
+
+struct PwSmem {
+  int4 stage[PW_STAGE];                   // 32 KB of output rows
+  unsigned long long pref[PR_TILE + 1];   // exclusive prefix of row counts per probe
+  int2 sprobe[PR_TILE];                   // the probe tuples
+  uint32_t run_lo[PR_TILE];               // run start (NULL_RUN: NULL-extended row)
+  uint16_t heavy[PR_TILE];                // probes expanded by the whole block
+  unsigned long long warp_tmp[PR_THREADS / 32 + 1];
+  unsigned long long tile_off;
+  unsigned int tile;
+  unsigned int nheavy;
+};
+
+__device__ __forceinline__ int4 make_row(const ej_table_view& t, uint32_t lo, uint32_t k, int2 s) {
+  if (lo == NULL_RUN) return make_int4(EJ_NULL_KEY, EJ_NULL_KEY, s.x, s.y);
+  return make_int4(__ldg(t.rkey + lo + k), s.y, s.x, s.y);
 }
 
 template <int KIND, bool OUTER>
 __global__ void __launch_bounds__(PR_THREADS)
-probe_write_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
-                   const unsigned long long* __restrict__ tile_off, uint64_t ntiles, ej_result* __restrict__ out,
-                   uint64_t cap, ej_dev_status* st) {
-  __shared__ unsigned long long warp_tmp[PR_THREADS / 32 + 1];
-  const uint64_t base = (uint64_t)blockIdx.x * PR_TILE;
-  const int* rv = reinterpret_cast<const int*>(t.rs) + 1;
-  int2 s[PR_ITEMS];
-  uint32_t lo[PR_ITEMS], hi[PR_ITEMS], m[PR_ITEMS];
-#pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    s[j] = idx < nP ? __ldcs(reinterpret_cast<const int2*>(P) + idx) : make_int2(0, 0);
+probe_write_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* lb_status,
+                   unsigned int* tile_ctr, uint64_t ntiles, ej_result* __restrict__ out, uint64_t cap,
+                   unsigned long long* d_total, ej_dev_status* st) {
+  extern __shared__ __align__(16) unsigned char pw_smem_raw[];
+  PwSmem& sm = *reinterpret_cast<PwSmem*>(pw_smem_raw);
+  if (threadIdx.x == 0) {
+    sm.tile = atomicAdd(tile_ctr, 1u);  // tiles claim ids in launch order (look-back progress)
+    sm.nheavy = 0;
   }
+  __syncthreads();
+  const uint64_t tile = sm.tile;
+  const uint64_t base = tile * PR_TILE;
+
+  // 1. runs of the tile's probes (probe p = j * 256 + thread, in S order)
+  uint32_t cnt[PR_ITEMS];
 #pragma unroll
   for (int j = 0; j < PR_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    lo[j] = hi[j] = 0;
-    if (idx < nP) Range<KIND>::find(t, s[j].y, lo[j], hi[j]);
-  }
-  unsigned long long c = 0;
-#pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    uint32_t k;
-    if (KIND == EJ_TABLE_SORTED) {
-      k = hi[j] - lo[j];
-    } else {
-      k = 0;
-      for (uint32_t i = lo[j]; i < hi[j]; i++) k += (__ldg(rv + 2 * (uint64_t)i) == s[j].y);
-    }
-    m[j] = k;
-    c += (OUTER && idx < nP && k == 0) ? 1u : k;
-  }
-  unsigned long long total;
-  unsigned long long pos = ej_block_exclusive_sum<PR_THREADS, unsigned long long>(c, warp_tmp, &total);
-  pos += tile_off[blockIdx.x];
-  if (blockIdx.x == 0 && threadIdx.x == 0 && tile_off[ntiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
-#pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    if (idx >= nP) continue;
-    if (OUTER && m[j] == 0) {
-      if (pos < cap) store_row(out, pos, EJ_NULL_KEY, EJ_NULL_KEY, s[j].x, s[j].y);
-      pos++;
-      continue;
-    }
-    if (m[j] == 0) continue;
-    for (uint32_t i = lo[j]; i < hi[j]; i++) {
-      const int2 r = __ldg(reinterpret_cast<const int2*>(t.rs) + i);
-      if (KIND == EJ_TABLE_SORTED || r.y == s[j].y) {
-        if (pos < cap) store_row(out, pos, r.x, r.y, s[j].x, s[j].y);
-        pos++;
+    const uint32_t p = (uint32_t)j * PR_THREADS + threadIdx.x;
+    const uint64_t idx = base + p;
+    int2 s = make_int2(0, 0);
+    uint32_t lo = NULL_RUN, c = 0;
+    if (idx < nP) {
+      s = __ldcs(reinterpret_cast<const int2*>(P) + idx);
+      EjRun<KIND>::find(t, s.y, lo, c);
+      if (OUTER && c == 0) {
+        c = 1;
+        lo = NULL_RUN;
       }
     }
+    sm.sprobe[p] = s;
+    sm.run_lo[p] = lo;
+    sm.pref[p] = c;
+    cnt[j] = c;
+    if (c > PW_LIGHT) sm.heavy[atomicAdd(&sm.nheavy, 1u)] = (uint16_t)p;
+  }
+  __syncthreads();
+
+  // 2. exclusive prefix of the counts in probe order (4 consecutive probes per thread)
+  unsigned long long a[PR_ITEMS], local = 0;
+#pragma unroll
+  for (int e = 0; e < PR_ITEMS; e++) {
+    a[e] = sm.pref[threadIdx.x * PR_ITEMS + e];
+    local += a[e];
+  }
+  unsigned long long total;
+  unsigned long long run = ej_block_exclusive_sum<PR_THREADS, unsigned long long>(local, sm.warp_tmp, &total);
+#pragma unroll
+  for (int e = 0; e < PR_ITEMS; e++) {
+    sm.pref[threadIdx.x * PR_ITEMS + e] = run;
+    run += a[e];
+  }
+  if (threadIdx.x == 0) sm.pref[PR_TILE] = total;
+
+  // 3. the tile's output offset from its predecessors
+  if (threadIdx.x < 32) {
+    const unsigned long long off = ej_lookback_warp(lb_status, tile, total, st, 3u);
+    if (threadIdx.x == 0) sm.tile_off = off;
+  }
+  __syncthreads();
+  const unsigned long long off = sm.tile_off;
+  if (threadIdx.x == 0 && tile == ntiles - 1) {
+    *d_total = off + total;
+    if (off + total > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  }
+  const unsigned int nheavy = sm.nheavy;
+
+  // 4. expand runs into rows, chunk by chunk, through shared memory
+  for (unsigned long long c0 = 0; c0 < total && off + c0 < cap; c0 += PW_STAGE) {
+    const unsigned long long cend = min(total, c0 + (unsigned long long)PW_STAGE);
+#pragma unroll
+    for (int j = 0; j < PR_ITEMS; j++) {
+      const uint32_t c = cnt[j];
+      if (c == 0 || c > PW_LIGHT) continue;
+      const uint32_t p = (uint32_t)j * PR_THREADS + threadIdx.x;
+      const unsigned long long pl = sm.pref[p];
+      if (pl + c <= c0 || pl >= cend) continue;
+      const int2 s = sm.sprobe[p];
+      const uint32_t lo = sm.run_lo[p];
+      for (uint32_t k = 0; k < c; k++) {
+        const unsigned long long o = pl + k;
+        if (o >= c0 && o < cend) sm.stage[o - c0] = make_row(t, lo, k, s);
+      }
+    }
+    for (unsigned int hh = 0; hh < nheavy; hh++) {
+      const uint32_t p = sm.heavy[hh];
+      const unsigned long long pl = sm.pref[p], pe = sm.pref[p + 1];
+      const unsigned long long lo_o = max(pl, c0), hi_o = min(pe, cend);
+      const int2 s = sm.sprobe[p];
+      const uint32_t lo = sm.run_lo[p];
+      for (unsigned long long o = lo_o + threadIdx.x; o < hi_o; o += PR_THREADS)
+        sm.stage[o - c0] = make_row(t, lo, (uint32_t)(o - pl), s);
+    }
+    __syncthreads();
+    const uint32_t n = (uint32_t)(cend - c0);
+    const unsigned long long g0 = off + c0;
+    for (uint32_t i = threadIdx.x; i < n; i += PR_THREADS)
+      if (g0 + i < cap) __stcs(reinterpret_cast<int4*>(out + g0 + i), sm.stage[i]);
+    __syncthreads();
   }
 }
 
@@ -221,9 +220,14 @@ ej_status launch_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* 
 
 template <int KIND, bool OUTER>
 ej_status launch_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                       const unsigned long long* toff, ej_result* out, uint64_t cap) {
-  probe_write_kernel<KIND, OUTER><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, toff, pp.ntiles,
-                                                                                    out, cap, h->d_status);
+                       ej_result* out, uint64_t cap, unsigned long long* d_total) {
+  unsigned long long* lb = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.lb_off));
+  unsigned int* ctr = reinterpret_cast<unsigned int*>(lb + pp.ntiles);
+  EJ_CUDA(h, cudaMemsetAsync(lb, 0, pp.ntiles * sizeof(unsigned long long) + 16, h->stream));
+  auto k = probe_write_kernel<KIND, OUTER>;
+  EJ_CUDA(h, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PwSmem)));
+  k<<<(unsigned)pp.ntiles, PR_THREADS, sizeof(PwSmem), h->stream>>>(P, pp.nP, t, lb, ctr, pp.ntiles, out, cap,
+                                                                     d_total, h->d_status);
   return ej_check_launch(h, "probe_write_kernel");
 }
 
@@ -239,19 +243,27 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta) {
 
 // ---- table build --------------------------------------------------------
 
+size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
+  return tp.kind == EJ_TABLE_HASH ? ((size_t(1) << tp.hb) + 1) * sizeof(uint32_t)
+                                  : (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
+}
+
+size_t ej_table_col_bytes(uint64_t nR) { return (size_t)(nR + EJ_TABLE_PAD) * sizeof(int32_t); }
+
 void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta) {
   tp.kind = kind;
   tp.nR = nR;
   tp.hb = kind == EJ_TABLE_HASH ? ej_table_bucket_bits(nR, delta) : 32u;
-  tp.passes = (tp.hb + 7) / 8;
+  tp.passes = 4;  // all 32 key bits: equal keys end up adjacent
   tp.nfence = (uint32_t)((nR + EJ_FENCE_STRIDE - 1) / EJ_FENCE_STRIDE);
-  const size_t tuples = (size_t)(nR ? nR : 1) * sizeof(ej_tuple);
   if (!own_storage) {
-    tp.rs_off = p.add(tuples);
-    if (kind == EJ_TABLE_HASH) tp.start_off = p.add(((size_t(1) << tp.hb) + 1) * sizeof(uint32_t));
-    else tp.start_off = p.add((size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t));
+    tp.rkey_off = p.add(ej_table_col_bytes(nR));
+    tp.rval_off = p.add(ej_table_col_bytes(nR));
+    tp.aux_off = p.add(ej_table_aux_bytes(tp));
   }
-  tp.tmp_off = p.add(tuples);
+  const size_t tuples = (size_t)(nR ? nR : 1) * sizeof(ej_tuple);
+  tp.tmp_a_off = p.add(tuples);
+  tp.tmp_b_off = p.add(tuples);
   ej_radix_plan_add(p, tp.rplan, nR);
 }
 
@@ -260,40 +272,41 @@ size_t ej_table_bytes(uint64_t nR, int delta) {
   return (size_t)nR * sizeof(ej_tuple) + ((size_t(1) << hb) + 1) * sizeof(uint32_t);
 }
 
-ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, ej_tuple* rs, void* aux,
-                         ej_table_view* view) {
-  ej_tuple* tmp = reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.tmp_off));
-  // LSD passes over the key, least significant digit first; the last pass
-  // writes rs.  Hash tables sort by the hb-bit bucket id (bits [32-hb, 32) of
-  // the hash); sorted indexes by all 32 bits of the order-preserving value.
-  const uint32_t lo_bit = 32u - tp.hb;
+ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, int32_t* rkey, int32_t* rval,
+                         void* aux, ej_table_view* view) {
+  // LSD passes over the 32-bit key (hash32(val), or the order-preserving image
+  // of val for a sorted index), least significant byte first; the last pass
+  // writes the two columns
   const int digit_kind = tp.kind == EJ_TABLE_HASH ? EJ_DIGIT_HASH : EJ_DIGIT_VALUE;
+  ej_tuple* tmp[2] = {reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.tmp_a_off)),
+                      reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.tmp_b_off))};
   const ej_tuple* src = R;
-  uint32_t done = 0;
-  for (uint32_t p = 0; p < tp.passes; p++) {
-    const uint32_t remaining = tp.hb - done;
-    const uint32_t bits = (remaining + (tp.passes - p) - 1) / (tp.passes - p);
-    ej_tuple* dst = ((tp.passes - 1 - p) % 2 == 0) ? rs : tmp;
-    if (tp.nR) EJ_TRY(ej_radix_pass(h, tp.rplan, src, dst, lo_bit + done, bits, digit_kind));
-    src = dst;
-    done += bits;
+  for (uint32_t p = 0; p < tp.passes && tp.nR; p++) {
+    const uint32_t shift = 8u * p;
+    if (p + 1 == tp.passes) {
+      EJ_TRY(ej_radix_pass_soa(h, tp.rplan, src, rkey, rval, shift, 8u, digit_kind));
+    } else {
+      EJ_TRY(ej_radix_pass(h, tp.rplan, src, tmp[p & 1], shift, 8u, digit_kind));
+      src = tmp[p & 1];
+    }
   }
   view->kind = tp.kind;
-  view->rs = rs;
+  view->rkey = rkey;
+  view->rval = rval;
   view->nR = tp.nR;
   view->hb = tp.hb;
   if (tp.kind == EJ_TABLE_HASH) {
     uint32_t* start = static_cast<uint32_t*>(aux);
     const uint64_t work = tp.nR + 1;
     const unsigned blocks = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)h->num_sms * 16);
-    bucket_start_kernel<<<blocks, 256, 0, h->stream>>>(rs, tp.nR, start, tp.hb);
+    bucket_start_kernel<<<blocks, 256, 0, h->stream>>>(rval, tp.nR, start, tp.hb);
     EJ_TRY(ej_check_launch(h, "bucket_start_kernel"));
     view->start = start;
   } else {
     int32_t* fence = static_cast<int32_t*>(aux);
     if (tp.nfence) {
       const unsigned blocks = (unsigned)std::min<uint64_t>((tp.nfence + 255) / 256, (uint64_t)h->num_sms * 16);
-      fence_kernel<<<blocks, 256, 0, h->stream>>>(rs, tp.nR, fence, tp.nfence);
+      fence_kernel<<<blocks, 256, 0, h->stream>>>(rval, fence, tp.nfence);
       EJ_TRY(ej_check_launch(h, "fence_kernel"));
     }
     view->fence = fence;
@@ -312,6 +325,7 @@ void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP) {
   pp.count_off = p.add((pp.ntiles + 1) * sizeof(unsigned long long));
   pp.off_off = p.add((pp.ntiles + 1) * sizeof(unsigned long long));
   pp.scan_off = p.add(ej_scan_scratch_bytes(pp.ntiles));
+  pp.lb_off = p.add(pp.ntiles * sizeof(unsigned long long) + 16);
 }
 
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
@@ -334,14 +348,16 @@ ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
 }
 
 ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                         bool outer, ej_result* out, uint64_t cap) {
-  if (!pp.ntiles) return EJ_OK;
-  const unsigned long long* toff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.off_off));
+                         bool outer, ej_result* out, uint64_t cap, unsigned long long* d_count) {
+  if (!pp.ntiles) {
+    EJ_CUDA(h, cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), h->stream));
+    return EJ_OK;
+  }
   if (t.kind == EJ_TABLE_HASH)
-    return outer ? launch_write<EJ_TABLE_HASH, true>(h, pp, P, t, toff, out, cap)
-                 : launch_write<EJ_TABLE_HASH, false>(h, pp, P, t, toff, out, cap);
-  return outer ? launch_write<EJ_TABLE_SORTED, true>(h, pp, P, t, toff, out, cap)
-               : launch_write<EJ_TABLE_SORTED, false>(h, pp, P, t, toff, out, cap);
+    return outer ? launch_write<EJ_TABLE_HASH, true>(h, pp, P, t, out, cap, d_count)
+                 : launch_write<EJ_TABLE_HASH, false>(h, pp, P, t, out, cap, d_count);
+  return outer ? launch_write<EJ_TABLE_SORTED, true>(h, pp, P, t, out, cap, d_count)
+               : launch_write<EJ_TABLE_SORTED, false>(h, pp, P, t, out, cap, d_count);
 }
 
 // ---- partition bits for the probe side ------------------------------------
@@ -372,10 +388,11 @@ void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint
   ej_probe_plan(p, L.pp, nS);
 }
 
-// Partition S (when the layout says so), count, scan and write; records
-// phase marks 2..4 (the caller has begun the set and marked the build).  The arena
-// must already hold the layout (reserved together with anything the table
-// placed there, so that no reservation moves a built table).
+// Partition S (when the layout says so), then either count (+ scan) or write
+// with look-back; records phase marks 2..4 (the caller has begun the set and
+// marked the build).  The arena must already hold the layout, reserved
+// together with anything the table placed there, so that no reservation
+// moves a built table.
 ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_view& t, const ej_tuple* S,
                         bool outer, bool count_only, ej_result* out, uint64_t out_cap,
                         unsigned long long* d_count) {
@@ -386,9 +403,13 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
     P = spart;
   }
   ej_phase_mark(h, 2);
-  EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
-  ej_phase_mark(h, 3);
-  if (!count_only) EJ_TRY(ej_probe_write(h, L.pp, P, t, outer, out, out_cap));
+  if (count_only) {
+    EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
+    ej_phase_mark(h, 3);
+  } else {
+    ej_phase_mark(h, 3);
+    EJ_TRY(ej_probe_write(h, L.pp, P, t, outer, out, out_cap, d_count));
+  }
   ej_phase_mark(h, 4);
   return EJ_OK;
 }
@@ -404,9 +425,9 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   ej_probe_layout_add(p, L, nS, pb);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
-  ej_tuple* rs = reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.rs_off));
   ej_table_view t;
-  EJ_TRY(ej_table_build(h, tp, R, rs, ej_arena_at(h, tp.start_off), &t));
+  EJ_TRY(ej_table_build(h, tp, R, reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rkey_off)),
+                        reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rval_off)), ej_arena_at(h, tp.aux_off), &t));
   ej_phase_mark(h, 1);
   return ej_probe_exec(h, L, t, S, /*outer=*/false, mode == 2, out, out_cap, d_count);
 }

@@ -10,17 +10,18 @@
 struct ej_table_plan_t {
   int kind = EJ_TABLE_HASH;
   uint64_t nR = 0;
-  uint32_t hb = 1;      // key bits sorted on (bucket bits; 32 for a sorted index)
-  uint32_t passes = 1;  // LSD radix passes
+  uint32_t hb = 1;      // bucket bits (hash tables)
+  uint32_t passes = 4;  // LSD radix passes over the 32-bit key
   uint32_t nfence = 0;  // sorted index: fence entries
-  size_t rs_off = 0, start_off = 0, tmp_off = 0;  // arena offsets (rs/start unused with own storage)
+  // arena offsets; rkey/rval/aux are unused when the table has its own storage
+  size_t rkey_off = 0, rval_off = 0, aux_off = 0, tmp_a_off = 0, tmp_b_off = 0;
   ej_radix_plan rplan;
 };
 
 struct ej_probe_plan_t {
   uint64_t nP = 0;
   uint64_t ntiles = 0;
-  size_t count_off = 0, off_off = 0, scan_off = 0;
+  size_t count_off = 0, off_off = 0, scan_off = 0, lb_off = 0;
 };
 
 struct ej_probe_layout {
@@ -31,19 +32,22 @@ struct ej_probe_layout {
 };
 
 size_t ej_table_bytes(uint64_t nR, int delta = 0);
+// bytes of one column (rkey or rval) including the vector-load padding
+size_t ej_table_col_bytes(uint64_t nR);
+// bytes of the bucket starts (hash) or the fence (sorted)
+size_t ej_table_aux_bytes(const ej_table_plan_t& tp);
 void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta = 0);
-// aux: bucket starts (hash, 2^hb+1 uint32) or fence (sorted, nfence int32)
-ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, ej_tuple* rs, void* aux,
-                         ej_table_view* view);
+ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, int32_t* rkey, int32_t* rval,
+                         void* aux, ej_table_view* view);
 
 uint64_t ej_probe_tiles(uint64_t nP);
 void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP);
-// count pass + scan; the total goes to *d_count (device) when d_count != nullptr
+// count kernel + scan; the total goes to *d_count (device) when d_count != nullptr
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                          bool outer, unsigned long long* d_count);
-// write pass; needs the offsets of ej_probe_count from the same plan
+// write kernel with look-back tile offsets; the total goes to *d_count
 ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                         bool outer, ej_result* out, uint64_t cap);
+                         bool outer, ej_result* out, uint64_t cap, unsigned long long* d_count);
 
 uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS);
 void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb);

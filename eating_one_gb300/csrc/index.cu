@@ -13,15 +13,24 @@
 #include "ej_device.cuh"
 #include "ej_entry.h"
 #include "hash_join.cuh"
+#include "probe.cuh"
 
 struct ej_index {
   int kind = EJ_TABLE_HASH;
   int device = 0;
   uint64_t nR = 0;
-  ej_tuple* rs = nullptr;  // device, owned
-  void* aux = nullptr;     // device, owned: bucket starts or fence
+  int32_t* rkey = nullptr;  // device, owned
+  int32_t* rval = nullptr;  // device, owned
+  void* aux = nullptr;      // device, owned: bucket starts or fence
   ej_table_view view;
 };
+
+static void index_release(ej_index* ix) {
+  cudaFree(ix->rkey);
+  cudaFree(ix->rval);
+  cudaFree(ix->aux);
+  delete ix;
+}
 
 // ---- index lifecycle ------------------------------------------------------
 
@@ -38,24 +47,19 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
   ix->kind = kind;
   ix->device = h->device;
   ix->nR = nR;
-  const size_t rs_bytes = (size_t)(nR ? nR : 1) * sizeof(ej_tuple);
-  const size_t aux_bytes = kind == EJ_TABLE_HASH ? ((size_t(1) << tp.hb) + 1) * sizeof(uint32_t)
-                                                 : (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
-  if (cudaMalloc(&ix->rs, rs_bytes) != cudaSuccess || cudaMalloc(&ix->aux, aux_bytes) != cudaSuccess) {
+  const size_t col = ej_table_col_bytes(nR), aux_bytes = ej_table_aux_bytes(tp);
+  if (cudaMalloc(&ix->rkey, col) != cudaSuccess || cudaMalloc(&ix->rval, col) != cudaSuccess ||
+      cudaMalloc(&ix->aux, aux_bytes) != cudaSuccess) {
     cudaGetLastError();
-    cudaFree(ix->rs);
-    cudaFree(ix->aux);
-    delete ix;
-    return ej_fail(h, EJ_ERR_NOMEM, "index storage of %zu bytes could not be allocated", rs_bytes + aux_bytes);
+    index_release(ix);
+    return ej_fail(h, EJ_ERR_NOMEM, "index storage of %zu bytes could not be allocated", 2 * col + aux_bytes);
   }
   ej_phase_begin(h);
-  ej_status st = ej_table_build(h, tp, R, ix->rs, ix->aux, &ix->view);
+  ej_status st = ej_table_build(h, tp, R, ix->rkey, ix->rval, ix->aux, &ix->view);
   for (int k = 1; k <= EJ_PHASES; k++) ej_phase_mark(h, k);
   if (st == EJ_OK) st = ej_finish(h, nullptr);
   if (st != EJ_OK) {
-    cudaFree(ix->rs);
-    cudaFree(ix->aux);
-    delete ix;
+    index_release(ix);
     return st;
   }
   *out = ix;
@@ -74,9 +78,7 @@ extern "C" ej_status ej_index_free(ej_handle* h, ej_index* idx) {
   if (!h || !idx) return EJ_ERR_INVALID;
   EJ_CUDA(h, cudaSetDevice(idx->device));
   EJ_CUDA(h, cudaStreamSynchronize(h->stream));
-  cudaFree(idx->rs);
-  cudaFree(idx->aux);
-  delete idx;
+  index_release(idx);
   return EJ_OK;
 }
 
@@ -162,8 +164,8 @@ extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t;
-  EJ_TRY(ej_table_build(h, tp, R, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.rs_off)),
-                        ej_arena_at(h, tp.start_off), &t));
+  EJ_TRY(ej_table_build(h, tp, R, reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rkey_off)),
+                        reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rval_off)), ej_arena_at(h, tp.aux_off), &t));
   ej_phase_mark(h, 1);
   EJ_TRY(ej_probe_exec(h, L, t, S, /*outer=*/true, false, out, out_cap, h->d_words));
   uint64_t count = 0;
@@ -180,19 +182,7 @@ constexpr int ST_THREADS = 256;
 constexpr int ST_ITEMS = 4;
 constexpr int ST_TILE = ST_THREADS * ST_ITEMS;
 
-__device__ __forceinline__ void bucket_range(const ej_table_view& t, int32_t v, uint32_t& lo, uint32_t& hi) {
-  const uint32_t b = ej_hash32((uint32_t)v) >> (32u - t.hb);
-  lo = __ldg(t.start + b);
-  hi = __ldg(t.start + b + 1);
-}
-
-__device__ __forceinline__ uint32_t bucket_matches(const ej_table_view& t, uint32_t lo, uint32_t hi, int32_t v) {
-  const int* rv = reinterpret_cast<const int*>(t.rs) + 1;
-  uint32_t m = 0;
-  for (uint32_t i = lo; i < hi; i++) m += (__ldg(rv + 2 * (uint64_t)i) == v);
-  return m;
-}
-
+// rows of fact row f: (matches of F1[f].val in D1) x (matches of F2[f].val in D2)
 __global__ void __launch_bounds__(ST_THREADS)
 star_count_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ F2, uint64_t nF, ej_table_view t1,
                   ej_table_view t2, unsigned long long* __restrict__ tile_count) {
@@ -203,13 +193,10 @@ star_count_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ 
   for (int j = 0; j < ST_ITEMS; j++) {
     const uint64_t idx = base + (uint64_t)j * ST_THREADS + threadIdx.x;
     if (idx >= nF) continue;
-    const int32_t v1 = __ldcs(&F1[idx].val), v2 = __ldcs(&F2[idx].val);
-    uint32_t lo1, hi1, lo2, hi2;
-    bucket_range(t1, v1, lo1, hi1);
-    bucket_range(t2, v2, lo2, hi2);
-    const uint32_t m1 = bucket_matches(t1, lo1, hi1, v1);
-    const uint32_t m2 = m1 ? bucket_matches(t2, lo2, hi2, v2) : 0u;
-    c += (unsigned long long)m1 * m2;
+    uint32_t lo1, c1, lo2, c2 = 0;
+    EjRun<EJ_TABLE_HASH>::find(t1, __ldcs(&F1[idx].val), lo1, c1);
+    if (c1) EjRun<EJ_TABLE_HASH>::find(t2, __ldcs(&F2[idx].val), lo2, c2);
+    c += (unsigned long long)c1 * c2;
   }
   unsigned long long total;
   ej_block_exclusive_sum<ST_THREADS, unsigned long long>(c, warp_tmp, &total);
@@ -223,21 +210,19 @@ star_write_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ 
   __shared__ unsigned long long warp_tmp[ST_THREADS / 32 + 1];
   const uint64_t base = (uint64_t)blockIdx.x * ST_TILE;
   int2 f1[ST_ITEMS], f2[ST_ITEMS];
-  uint32_t lo1[ST_ITEMS], hi1[ST_ITEMS], lo2[ST_ITEMS], hi2[ST_ITEMS];
+  uint32_t lo1[ST_ITEMS], c1[ST_ITEMS], lo2[ST_ITEMS], c2[ST_ITEMS];
   unsigned long long c = 0;
 #pragma unroll
   for (int j = 0; j < ST_ITEMS; j++) {
     const uint64_t idx = base + (uint64_t)j * ST_THREADS + threadIdx.x;
-    lo1[j] = hi1[j] = lo2[j] = hi2[j] = 0;
+    c1[j] = c2[j] = lo1[j] = lo2[j] = 0;
+    f1[j] = f2[j] = make_int2(0, 0);
     if (idx >= nF) continue;
     f1[j] = __ldcs(reinterpret_cast<const int2*>(F1) + idx);
     f2[j] = __ldcs(reinterpret_cast<const int2*>(F2) + idx);
-    bucket_range(t1, f1[j].y, lo1[j], hi1[j]);
-    bucket_range(t2, f2[j].y, lo2[j], hi2[j]);
-    const uint32_t m1 = bucket_matches(t1, lo1[j], hi1[j], f1[j].y);
-    const uint32_t m2 = m1 ? bucket_matches(t2, lo2[j], hi2[j], f2[j].y) : 0u;
-    if (m2 == 0) hi1[j] = lo1[j];  // nothing to write for this fact row
-    c += (unsigned long long)m1 * m2;
+    EjRun<EJ_TABLE_HASH>::find(t1, f1[j].y, lo1[j], c1[j]);
+    if (c1[j]) EjRun<EJ_TABLE_HASH>::find(t2, f2[j].y, lo2[j], c2[j]);
+    c += (unsigned long long)c1[j] * c2[j];
   }
   unsigned long long total;
   unsigned long long pos = ej_block_exclusive_sum<ST_THREADS, unsigned long long>(c, warp_tmp, &total);
@@ -245,16 +230,14 @@ star_write_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ 
   if (blockIdx.x == 0 && threadIdx.x == 0 && tile_off[ntiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
 #pragma unroll
   for (int j = 0; j < ST_ITEMS; j++) {
-    for (uint32_t a = lo1[j]; a < hi1[j]; a++) {
-      const int2 d1 = __ldg(reinterpret_cast<const int2*>(t1.rs) + a);
-      if (d1.y != f1[j].y) continue;
-      for (uint32_t b = lo2[j]; b < hi2[j]; b++) {
-        const int2 d2 = __ldg(reinterpret_cast<const int2*>(t2.rs) + b);
-        if (d2.y != f2[j].y) continue;
+    if (!c2[j]) continue;
+    for (uint32_t a = 0; a < c1[j]; a++) {
+      const int32_t k1 = __ldg(t1.rkey + lo1[j] + a);
+      for (uint32_t b = 0; b < c2[j]; b++) {
         if (pos < cap) {
           int4* o = reinterpret_cast<int4*>(out + pos);
-          __stcs(o, make_int4(d1.x, d1.y, f1[j].x, f1[j].y));
-          __stcs(o + 1, make_int4(d2.x, d2.y, f2[j].x, f2[j].y));
+          __stcs(o, make_int4(k1, f1[j].y, f1[j].x, f1[j].y));
+          __stcs(o + 1, make_int4(__ldg(t2.rkey + lo2[j] + b), f2[j].y, f2[j].x, f2[j].y));
         }
         pos++;
       }
@@ -284,10 +267,10 @@ extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tu
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t1, t2;
-  EJ_TRY(ej_table_build(h, tp1, D1, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp1.rs_off)),
-                        ej_arena_at(h, tp1.start_off), &t1));
-  EJ_TRY(ej_table_build(h, tp2, D2, reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp2.rs_off)),
-                        ej_arena_at(h, tp2.start_off), &t2));
+  EJ_TRY(ej_table_build(h, tp1, D1, reinterpret_cast<int32_t*>(ej_arena_at(h, tp1.rkey_off)),
+                        reinterpret_cast<int32_t*>(ej_arena_at(h, tp1.rval_off)), ej_arena_at(h, tp1.aux_off), &t1));
+  EJ_TRY(ej_table_build(h, tp2, D2, reinterpret_cast<int32_t*>(ej_arena_at(h, tp2.rkey_off)),
+                        reinterpret_cast<int32_t*>(ej_arena_at(h, tp2.rval_off)), ej_arena_at(h, tp2.aux_off), &t2));
   ej_phase_mark(h, 1);
   ej_phase_mark(h, 2);
   unsigned long long* tcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, count_off));

@@ -5,16 +5,16 @@
 // rpartitioning, driven by hj.cc:430-534 and :702-829): 16-thread blocks that
 // each walk 256 consecutive tuples, one 6-bit digit per pass, a host
 // round-trip per pass.  Here one pass is three launches on the stream:
-//   1. rx_hist_kernel    per 8192-tuple tile, digit counts in shared memory
-//                        (warp-aggregated with __match_any_sync, so skewed
-//                        digits do not serialise on atomics), stored
-//                        digit-major: hist[digit * ntiles + tile];
+//   1. rx_hist_kernel    per 8192-tuple tile, digit counts in warp-private
+//                        shared-memory histograms, stored digit-major:
+//                        hist[digit * ntiles + tile];
 //   2. look-back scan    of the digit-major histogram gives every (digit, tile)
 //                        its global output offset (scan.cu);
 //   3. rx_scatter_kernel stages the tile in shared memory, ranks it stably by
-//                        digit (warp-ordered match_any ranking), and writes it
-//                        digit run by digit run, so consecutive threads store
-//                        consecutive addresses.
+//                        digit (warp-ordered ranking; the lanes sharing a
+//                        digit come from one ballot per digit bit), and writes
+//                        it digit run by digit run, so consecutive threads
+//                        store consecutive addresses.
 // Digits are up to 8 bits of hash32(val).  Positions are 32-bit: n < 2^32.
 #include "ej_device.cuh"
 
@@ -50,14 +50,12 @@ rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, uint32_t* __restrict
     const uint64_t idx = wbase + (uint64_t)r * 32u + lane;
     v[r] = idx < n ? __ldcs(vals + 2 * idx) : 0;
   }
+  // warp-private histograms: counting order does not matter, so plain
+  // shared-memory atomics (same-digit lanes of one instruction serialise in hardware)
 #pragma unroll
   for (int r = 0; r < RX_ROUNDS; r++) {
     const uint64_t idx = wbase + (uint64_t)r * 32u + lane;
-    const bool valid = idx < n;
-    const uint32_t d = valid ? rx_digit<KIND>(v[r], shift, mask) : 0xFFFFFFFFu;
-    const unsigned int peers = __match_any_sync(EJ_FULL_MASK, d);
-    if (valid && lane == (unsigned)(__ffs(peers) - 1)) cnt[warp][d] += __popc(peers);
-    __syncwarp();
+    if (idx < n) atomicAdd(&cnt[warp][rx_digit<KIND>(v[r], shift, mask)], 1u);
   }
   __syncthreads();
   for (uint32_t d = threadIdx.x; d < ndig; d += RX_THREADS) {
@@ -71,15 +69,19 @@ rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, uint32_t* __restrict
 struct RxScatterSmem {
   ej_tuple tile[RX_TILE];              // 64 KB
   uint16_t perm[RX_TILE];              // 16 KB: sorted position -> tile index
+  uint8_t dtile[RX_TILE];              // 8 KB: digit of each tile index
   uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];  // 8 KB
   uint32_t digit_start[RX_MAX_DIGITS];
   uint32_t gbase[RX_MAX_DIGITS];
   uint32_t warp_tmp[RX_WARPS + 1];
 };
 
-template <int KIND>
+// SOA: write the key and val of each tuple to two separate arrays (the last
+// pass of a table build) instead of tuples
+template <int KIND, bool SOA>
 __global__ void __launch_bounds__(RX_THREADS)
 rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, ej_tuple* __restrict__ out,
+                  int32_t* __restrict__ out_keys, int32_t* __restrict__ out_vals,
                   const uint32_t* __restrict__ offs, uint32_t ntiles, uint32_t shift, uint32_t mask) {
   extern __shared__ __align__(16) unsigned char rx_smem_raw[];
   RxScatterSmem& sm = *reinterpret_cast<RxScatterSmem*>(rx_smem_raw);
@@ -96,15 +98,17 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, ej_tuple* __restr
   for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&sm.cnt[0][0])[i] = 0u;
   __syncthreads();
 
-  // 2. per-warp digit counts over the warp's consecutive span
+  // 2. digits of the tile (kept in shared memory) and per-warp digit counts
+  //    over the warp's consecutive span; counting order does not matter
   const uint32_t wbase = warp * RX_WARP_SPAN;
+#pragma unroll 4
   for (int r = 0; r < RX_ROUNDS; r++) {
     const uint32_t i = wbase + r * 32u + lane;
-    const bool valid = i < tile_n;
-    const uint32_t d = valid ? rx_digit<KIND>(sm.tile[i].val, shift, mask) : 0xFFFFFFFFu;
-    const unsigned int peers = __match_any_sync(EJ_FULL_MASK, d);
-    if (valid && lane == (unsigned)(__ffs(peers) - 1)) sm.cnt[warp][d] += __popc(peers);
-    __syncwarp();
+    if (i < tile_n) {
+      const uint32_t d = rx_digit<KIND>(sm.tile[i].val, shift, mask);
+      sm.dtile[i] = (uint8_t)d;
+      atomicAdd(&sm.cnt[warp][d], 1u);
+    }
   }
   __syncthreads();
 
@@ -127,19 +131,20 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, ej_tuple* __restr
   }
   __syncthreads();
 
-  // 4. stable rank: warp order, then round order, then lane order
+  // 4. stable rank: warp order, then round order, then lane order; the lanes
+  //    sharing a digit are found with one ballot per digit bit
   for (int r = 0; r < RX_ROUNDS; r++) {
     const uint32_t i = wbase + r * 32u + lane;
     const bool valid = i < tile_n;
-    const uint32_t d = valid ? rx_digit<KIND>(sm.tile[i].val, shift, mask) : 0xFFFFFFFFu;
-    const unsigned int peers = __match_any_sync(EJ_FULL_MASK, d);
+    const uint32_t d = valid ? sm.dtile[i] : 0u;
+    const unsigned int peers = ej_match_digit<8>(d, __ballot_sync(EJ_FULL_MASK, valid));
     const int leader = __ffs(peers) - 1;
     uint32_t old = 0;
     if (valid && (int)lane == leader) {
       old = sm.cnt[warp][d];
       sm.cnt[warp][d] = old + __popc(peers);
     }
-    old = __shfl_sync(EJ_FULL_MASK, old, leader);
+    old = __shfl_sync(EJ_FULL_MASK, old, leader < 0 ? 0 : leader);
     if (valid) sm.perm[sm.digit_start[d] + old + __popc(peers & ej_lanemask_lt())] = (uint16_t)i;
     __syncwarp();
   }
@@ -147,9 +152,15 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, ej_tuple* __restr
 
   // 5. write digit runs: sorted position k goes to gbase[digit] + k
   for (uint32_t k = threadIdx.x; k < tile_n; k += RX_THREADS) {
-    const ej_tuple t = sm.tile[sm.perm[k]];
-    const uint32_t d = rx_digit<KIND>(t.val, shift, mask);
-    reinterpret_cast<uint2*>(out)[sm.gbase[d] + k] = make_uint2((uint32_t)t.key, (uint32_t)t.val);
+    const uint32_t i = sm.perm[k];
+    const ej_tuple t = sm.tile[i];
+    const uint32_t pos = sm.gbase[sm.dtile[i]] + k;
+    if (SOA) {
+      out_keys[pos] = t.key;
+      out_vals[pos] = t.val;
+    } else {
+      reinterpret_cast<uint2*>(out)[pos] = make_uint2((uint32_t)t.key, (uint32_t)t.val);
+    }
   }
 }
 
@@ -166,9 +177,9 @@ void ej_radix_plan_add(ej_plan_bytes& p, ej_radix_plan& rp, uint64_t n) {
   rp.scan_off = p.add(ej_scan_scratch_bytes(cells));
 }
 
-template <int KIND>
+template <int KIND, bool SOA>
 static ej_status radix_pass_kind(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
-                                 uint32_t shift, uint32_t bits) {
+                                 int32_t* out_keys, int32_t* out_vals, uint32_t shift, uint32_t bits) {
   const uint32_t mask = (1u << bits) - 1u;
   const uint64_t cells = (uint64_t)rp.ntiles << bits;
   uint32_t* hist = reinterpret_cast<uint32_t*>(ej_arena_at(h, rp.hist_off));
@@ -176,18 +187,33 @@ static ej_status radix_pass_kind(ej_handle* h, const ej_radix_plan& rp, const ej
   rx_hist_kernel<KIND><<<rp.ntiles, RX_THREADS, 0, h->stream>>>(in, rp.n, hist, rp.ntiles, shift, mask);
   EJ_TRY(ej_check_launch(h, "rx_hist_kernel"));
   EJ_TRY(ej_scan_u32_u32(h, hist, cells, offs, ej_arena_at(h, rp.scan_off)));
-  EJ_CUDA(h, cudaFuncSetAttribute(rx_scatter_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  EJ_CUDA(h, cudaFuncSetAttribute(rx_scatter_kernel<KIND, SOA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(RxScatterSmem)));
-  rx_scatter_kernel<KIND><<<rp.ntiles, RX_THREADS, sizeof(RxScatterSmem), h->stream>>>(in, rp.n, out, offs,
-                                                                                       rp.ntiles, shift, mask);
+  rx_scatter_kernel<KIND, SOA><<<rp.ntiles, RX_THREADS, sizeof(RxScatterSmem), h->stream>>>(
+      in, rp.n, out, out_keys, out_vals, offs, rp.ntiles, shift, mask);
   return ej_check_launch(h, "rx_scatter_kernel");
+}
+
+static ej_status check_digit(ej_handle* h, uint32_t shift, uint32_t bits) {
+  if (bits == 0 || bits > 8 || shift + bits > 32)
+    return ej_fail(h, EJ_ERR_INTERNAL, "radix pass: bad digit (shift %u, bits %u)", shift, bits);
+  return EJ_OK;
 }
 
 ej_status ej_radix_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
                         uint32_t shift, uint32_t bits, int digit_kind) {
   if (rp.n == 0) return EJ_OK;
-  if (bits == 0 || bits > 8 || shift + bits > 32)
-    return ej_fail(h, EJ_ERR_INTERNAL, "radix pass: bad digit (shift %u, bits %u)", shift, bits);
-  if (digit_kind == EJ_DIGIT_VALUE) return radix_pass_kind<EJ_DIGIT_VALUE>(h, rp, in, out, shift, bits);
-  return radix_pass_kind<EJ_DIGIT_HASH>(h, rp, in, out, shift, bits);
+  EJ_TRY(check_digit(h, shift, bits));
+  if (digit_kind == EJ_DIGIT_VALUE)
+    return radix_pass_kind<EJ_DIGIT_VALUE, false>(h, rp, in, out, nullptr, nullptr, shift, bits);
+  return radix_pass_kind<EJ_DIGIT_HASH, false>(h, rp, in, out, nullptr, nullptr, shift, bits);
+}
+
+ej_status ej_radix_pass_soa(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, int32_t* out_keys,
+                            int32_t* out_vals, uint32_t shift, uint32_t bits, int digit_kind) {
+  if (rp.n == 0) return EJ_OK;
+  EJ_TRY(check_digit(h, shift, bits));
+  if (digit_kind == EJ_DIGIT_VALUE)
+    return radix_pass_kind<EJ_DIGIT_VALUE, true>(h, rp, in, nullptr, out_keys, out_vals, shift, bits);
+  return radix_pass_kind<EJ_DIGIT_HASH, true>(h, rp, in, nullptr, out_keys, out_vals, shift, bits);
 }
