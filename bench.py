@@ -189,6 +189,81 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case(name: str, scale: int, repeat: int) -> None:
+    """A small case for profilers: `repeat` hash joins of one workload at
+    1/2^scale size, each synchronised; prints the phase times of the last."""
+    import torch
+
+    from eating_one_gb300.build import build
+    from eating_one_gb300.engine import Engine
+    from eating_one_gb300.workloads import workload
+
+    build()
+    eng = Engine(0)
+    w = workload(name, scale)
+    R, S = eng.generate(w["R"]), eng.generate(w["S"])
+    n_out = eng.count("hash", R, S)
+    out = torch.empty((n_out, 4), dtype=torch.int32, device="cuda")
+    eng.set_timing(True)
+    for _ in range(repeat):
+        got = eng.hash_join(R, S, out=out)
+        assert got.shape[0] == n_out
+    print(json.dumps({"profile_case": name, "scale": scale, "R": int(R.shape[0]), "S": int(S.shape[0]),
+                      "rows": n_out, "phases_ms": [round(x, 4) for x in eng.phase_ms()]}), flush=True)
+
+
+def run_serve(n_requests: int, n_instances: int, lanes: int) -> None:
+    """Configuration C5: the served request stream, batched vs one pipeline per join.
+
+    Both modes first run the whole stream submitted at once (saturation); then
+    Poisson arrivals at 0.25, 0.5, 1, 2 and 4 times the per-join saturation
+    rate.  At equal p99 (the per-join p99 at half its saturation rate), the
+    ratio of the highest throughputs each mode sustains is reported."""
+    import torch
+
+    from eating_one_gb300.build import build
+    from eating_one_gb300.engine import Engine
+    from eating_one_gb300.serve import BATCHED, PER_JOIN, RequestPool, Server, run_stream
+
+    build()
+    eng = Engine(0)
+    pool = RequestPool(eng, n_instances)
+    modes = {"batched": BATCHED, "per_join": PER_JOIN}
+    res = {m: {} for m in modes}
+    for name, mode in modes.items():
+        srv = Server(mode, lanes=lanes)
+        run_stream(srv, pool, min(200, n_requests), None, seed=7)  # warm-up: arenas grow once
+        res[name]["saturation"] = run_stream(srv, pool, n_requests, None, seed=8)
+        srv.close()
+    base_rate = res["per_join"]["saturation"]["requests_per_s"]
+    sweep = [0.25, 0.5, 1.0, 2.0, 4.0]
+    for name, mode in modes.items():
+        srv = Server(mode, lanes=lanes)
+        run_stream(srv, pool, min(200, n_requests), None, seed=7)
+        res[name]["poisson"] = [run_stream(srv, pool, n_requests, f * base_rate, seed=10 + i)
+                                for i, f in enumerate(sweep)]
+        srv.close()
+    target = res["per_join"]["poisson"][1]["p99_ms"]
+
+    def best(name):
+        ok = [r for r in res[name]["poisson"] if r["p99_ms"] <= target] + \
+             ([res[name]["saturation"]] if res[name]["saturation"]["p99_ms"] <= target else [])
+        return max((r["tuples_per_s"] for r in ok), default=0.0)
+
+    wrong = sum(r["wrong"] for m in res.values() for r in [m["saturation"]] + m["poisson"])
+    line = {"workload": "C5 served stream: %d requests, |R| log-uniform in [2^10, 2^22], |S| = 4|R|, u in {1,2,8}, "
+                        "Poisson arrivals; %d device-resident request instances" % (n_requests, n_instances),
+            "lanes": lanes, "per_join_saturation_requests_per_s": base_rate, "sweep_factors": sweep,
+            "p99_target_ms": target, "results": res,
+            "throughput_at_equal_p99": {"batched": best("batched"), "per_join": best("per_join"),
+                                        "ratio": best("batched") / max(best("per_join"), 1e-9)},
+            "saturation_ratio": res["batched"]["saturation"]["tuples_per_s"] /
+                                res["per_join"]["saturation"]["tuples_per_s"],
+            "wrong_results": wrong}
+    print(json.dumps(line), flush=True)
+    del torch
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -197,8 +272,21 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", default=None, help="run a small profiling case of this workload instead")
+    ap.add_argument("--scale", type=int, default=3)
+    ap.add_argument("--repeat", type=int, default=3)
+    ap.add_argument("--serve", action="store_true", help="run the served-stream sweep (configuration C5)")
+    ap.add_argument("--requests", type=int, default=10000)
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--lanes", type=int, default=2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.serve:
+        run_serve(args.requests, args.instances, args.lanes)
+        return
+    if args.profile:
+        run_profile_case(args.profile, args.scale, args.repeat)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

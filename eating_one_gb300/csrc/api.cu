@@ -97,6 +97,8 @@ extern "C" ej_status ej_destroy(ej_handle* h) {
   cudaFree(h->zipf.d_cdf);
   cudaFreeHost(h->h_words);
   cudaFreeHost(h->h_status);
+  cudaFree(h->d_batch_counts);
+  cudaFreeHost(h->h_batch_counts);
   for (cudaEvent_t e : h->ring) cudaEventDestroy(e);
   delete h;
   return EJ_OK;

@@ -1,0 +1,269 @@
+// batch.cu - many hash joins as one pipeline.
+//
+// The reference runs one join per process, every phase its own launch with a
+// host synchronisation after it (joins/hashJoin_gpu/main_street/hj.cc:454-475).
+// For a stream of joins of uneven sizes (most of them small) that is launch-
+// and latency-bound.  Here a batch of joins is one fixed sequence of launches,
+// whatever the number of joins in it:
+//   gather      every R into one concatenated array (one launch over R tiles)
+//   build       four segmented LSD radix passes: tiles never cross a join and
+//               the digit histograms are laid out join by join, so one scan
+//               places every join's rows in its own range, hash-sorted
+//   starts      every join's bucket starts in one launch (its own bucket bits)
+//   write       one launch over every join's probe tiles: a tile claims the
+//               next id of a global work queue (join order), probes its own
+//               join's table and chains its output offset by look-back only
+//               within its join; the last tile of a join stores its count.
+// Every join's rows are bitwise the same as when it runs alone: the same
+// table order (stable passes over the same rows) and the same tile order.
+#include "ej_device.cuh"
+#include "ej_entry.h"
+#include "hash_join.cuh"
+#include "probe_write.cuh"
+
+namespace {
+
+constexpr uint32_t BX_RX_TILE = EJ_RX_TILE;
+
+// per join, on the device
+struct BatchJoin {
+  ej_table_view view;
+  const ej_tuple* S;
+  ej_result* out;
+  unsigned long long cap;
+  unsigned long long* d_count;
+  unsigned long long nS;
+  uint32_t first_ptile;  // first probe tile (global work-queue index)
+  uint32_t nptiles;
+  unsigned long long r_row0;  // first row of the join in the concatenated R
+  const ej_tuple* R;
+};
+
+// global probe tile -> (join, tile of the join)
+struct BatchPTile {
+  uint32_t join, local;
+};
+
+__global__ void batch_gather_kernel(const ej_rx_tile* __restrict__ tiles, const BatchJoin* __restrict__ joins,
+                                    ej_tuple* __restrict__ rcat) {
+  const ej_rx_tile d = tiles[blockIdx.x];
+  const BatchJoin& j = joins[d.pad];
+  const uint2* src = reinterpret_cast<const uint2*>(j.R) + (d.start - j.r_row0);
+  uint2* dst = reinterpret_cast<uint2*>(rcat) + d.start;
+  for (uint32_t i = threadIdx.x; i < d.n; i += blockDim.x) dst[i] = __ldcs(src + i);
+}
+
+// bucket starts of every join: the block of one R tile fills the gaps
+// between the buckets of consecutive rows of its join; the join's last row
+// also fills the tail up to 2^hb
+__global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, const BatchJoin* __restrict__ joins,
+                                          uint32_t* __restrict__ start_all, const unsigned long long* start_base) {
+  const ej_rx_tile d = tiles[blockIdx.x];
+  const BatchJoin& j = joins[d.pad];
+  const ej_table_view& t = j.view;
+  uint32_t* start = start_all + start_base[d.pad];
+  const uint64_t first = d.start - j.r_row0;  // local row index of the tile's first row
+  const int64_t nb = (int64_t)1 << t.hb;
+  for (uint32_t i = threadIdx.x; i < d.n; i += blockDim.x) {
+    const uint64_t r = first + i;
+    const int64_t cur = (int64_t)ej_bucket_of(t.rval[r], t.hb);
+    const int64_t prev = r > 0 ? (int64_t)ej_bucket_of(t.rval[r - 1], t.hb) : -1;
+    for (int64_t b = prev + 1; b <= cur; b++) start[b] = (uint32_t)r;
+    if (r + 1 == t.nR)
+      for (int64_t b = cur + 1; b <= nb; b++) start[b] = (uint32_t)t.nR;
+  }
+}
+
+__global__ void __launch_bounds__(PR_THREADS, 4)
+batch_write_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
+                   unsigned long long* lb_status, unsigned int* tile_ctr, ej_dev_status* st) {
+  extern __shared__ __align__(16) unsigned char bw_smem_raw[];
+  PwSmem& sm = *reinterpret_cast<PwSmem*>(bw_smem_raw);
+  if (threadIdx.x == 0) {
+    sm.tile = atomicAdd(tile_ctr, 1u);  // global work queue, join by join
+  }
+  __syncthreads();
+  const BatchPTile pt = ptiles[sm.tile];
+  const BatchJoin& j = joins[pt.join];
+  ej_probe_write_tile<EJ_TABLE_HASH, false>(sm, j.S, (uint64_t)pt.local * PR_TILE, j.nS, j.view,
+                                            lb_status + j.first_ptile, pt.local, pt.local + 1 == j.nptiles, j.out,
+                                            j.cap, j.d_count, st);
+}
+
+}  // namespace
+
+// Plan and launch; counts go to d_counts[i] (device).
+static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, unsigned long long* d_counts) {
+  // host-side layout of the batch
+  std::vector<BatchJoin> joins(n);
+  std::vector<ej_rx_tile> rtiles;
+  std::vector<BatchPTile> ptiles;
+  std::vector<unsigned long long> sbase(n);
+  uint64_t nr_total = 0, start_total = 0, cells = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint64_t nR = jd[i].nR, nS = jd[i].nS;
+    BatchJoin& b = joins[i];
+    b.R = jd[i].R;
+    b.S = jd[i].S;
+    b.nS = nS;
+    b.out = jd[i].out;
+    b.cap = jd[i].out_cap;
+    b.d_count = d_counts + i;
+    b.r_row0 = nr_total;
+    b.view.kind = EJ_TABLE_HASH;
+    b.view.nR = nR;
+    b.view.hb = ej_table_bucket_bits(nR, h->opt_bucket_delta);
+    const uint32_t rt = (uint32_t)((nR + BX_RX_TILE - 1) / BX_RX_TILE);
+    for (uint32_t t = 0; t < rt; t++) {
+      ej_rx_tile d;
+      d.start = nr_total + (uint64_t)t * BX_RX_TILE;
+      d.n = (uint32_t)std::min<uint64_t>(BX_RX_TILE, nR - (uint64_t)t * BX_RX_TILE);
+      d.cell0 = (uint32_t)(cells + t);
+      d.stride = rt;
+      d.pad = i;
+      rtiles.push_back(d);
+    }
+    cells += (uint64_t)rt * 256;
+    sbase[i] = start_total;
+    start_total += (1ull << b.view.hb) + 1;
+    b.first_ptile = (uint32_t)ptiles.size();
+    b.nptiles = (uint32_t)((nS + PR_TILE - 1) / PR_TILE);
+    for (uint32_t t = 0; t < b.nptiles; t++) ptiles.push_back({i, t});
+    nr_total += nR;
+  }
+  if (cells > 0xFFFFFFFFull || nr_total >= 0xFFFFFFFFull)
+    return ej_fail(h, EJ_ERR_TOO_LARGE, "batch of %llu R rows is too large", (unsigned long long)nr_total);
+
+  // arena layout
+  ej_plan_bytes p;
+  const size_t joins_off = p.add(n * sizeof(BatchJoin));
+  const size_t rtiles_off = p.add(std::max<size_t>(rtiles.size(), 1) * sizeof(ej_rx_tile));
+  const size_t ptiles_off = p.add(std::max<size_t>(ptiles.size(), 1) * sizeof(BatchPTile));
+  const size_t sbase_off = p.add(n * sizeof(unsigned long long));
+  const size_t rcat_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
+  const size_t tmpa_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
+  const size_t tmpb_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
+  const size_t rkey_off = p.add(ej_table_col_bytes(nr_total));
+  const size_t rval_off = p.add(ej_table_col_bytes(nr_total));
+  const size_t start_off = p.add(start_total * sizeof(uint32_t));
+  ej_radix_plan rp;
+  rp.n = nr_total;
+  rp.ntiles = (uint32_t)rtiles.size();
+  rp.hist_off = p.add(cells * sizeof(uint32_t));
+  rp.offs_off = p.add((cells + 1) * sizeof(uint32_t));
+  rp.scan_off = p.add(ej_scan_scratch_bytes(cells));
+  const size_t lb_off = p.add(ptiles.size() * sizeof(unsigned long long) + 16);
+  EJ_TRY(ej_arena_reserve(h, p.bytes));
+
+  char* A = static_cast<char*>(h->arena);
+  int32_t* rkey = reinterpret_cast<int32_t*>(A + rkey_off);
+  int32_t* rval = reinterpret_cast<int32_t*>(A + rval_off);
+  uint32_t* start = reinterpret_cast<uint32_t*>(A + start_off);
+  for (uint32_t i = 0; i < n; i++) {
+    BatchJoin& b = joins[i];
+    b.view.rkey = rkey + b.r_row0;
+    b.view.rval = rval + b.r_row0;
+    b.view.voff = (uint32_t)(b.r_row0 & 3u);  // the arena column is 16-byte aligned
+    b.view.start = start + sbase[i];
+  }
+  // descriptors go up with the batch (stream-ordered copies)
+  const size_t jb = n * sizeof(BatchJoin), rb = rtiles.size() * sizeof(ej_rx_tile),
+               pb = ptiles.size() * sizeof(BatchPTile), sb = n * sizeof(unsigned long long);
+  EJ_CUDA(h, cudaMemcpyAsync(A + joins_off, joins.data(), jb, cudaMemcpyHostToDevice, h->stream));
+  if (rb) EJ_CUDA(h, cudaMemcpyAsync(A + rtiles_off, rtiles.data(), rb, cudaMemcpyHostToDevice, h->stream));
+  if (pb) EJ_CUDA(h, cudaMemcpyAsync(A + ptiles_off, ptiles.data(), pb, cudaMemcpyHostToDevice, h->stream));
+  EJ_CUDA(h, cudaMemcpyAsync(A + sbase_off, sbase.data(), sb, cudaMemcpyHostToDevice, h->stream));
+  EJ_CUDA(h, cudaMemsetAsync(d_counts, 0, n * sizeof(unsigned long long), h->stream));
+  const BatchJoin* djoins = reinterpret_cast<const BatchJoin*>(A + joins_off);
+  const ej_rx_tile* drt = reinterpret_cast<const ej_rx_tile*>(A + rtiles_off);
+  rp.tiles = drt;
+
+  ej_phase_begin(h);
+  if (!rtiles.empty()) {
+    ej_tuple* rcat = reinterpret_cast<ej_tuple*>(A + rcat_off);
+    batch_gather_kernel<<<(unsigned)rtiles.size(), 256, 0, h->stream>>>(drt, djoins, rcat);
+    EJ_TRY(ej_check_launch(h, "batch_gather_kernel"));
+    ej_tuple* tmp[2] = {reinterpret_cast<ej_tuple*>(A + tmpa_off), reinterpret_cast<ej_tuple*>(A + tmpb_off)};
+    const ej_tuple* src = rcat;
+    for (uint32_t pass = 0; pass < 4; pass++) {
+      if (pass == 3) {
+        EJ_TRY(ej_radix_pass_soa(h, rp, src, rkey, rval, 24u, 8u, EJ_DIGIT_HASH));
+      } else {
+        EJ_TRY(ej_radix_pass(h, rp, src, tmp[pass & 1], 8u * pass, 8u, EJ_DIGIT_HASH));
+        src = tmp[pass & 1];
+      }
+    }
+  }
+  // joins with an empty R keep all-zero bucket starts
+  EJ_CUDA(h, cudaMemsetAsync(start, 0, start_total * sizeof(uint32_t), h->stream));
+  if (!rtiles.empty()) {
+    batch_bucket_start_kernel<<<(unsigned)rtiles.size(), 256, 0, h->stream>>>(
+        drt, djoins, start, reinterpret_cast<const unsigned long long*>(A + sbase_off));
+    EJ_TRY(ej_check_launch(h, "batch_bucket_start_kernel"));
+  }
+  ej_phase_mark(h, 1);
+  ej_phase_mark(h, 2);
+  ej_phase_mark(h, 3);
+  if (!ptiles.empty()) {
+    unsigned long long* lb = reinterpret_cast<unsigned long long*>(A + lb_off);
+    EJ_CUDA(h, cudaMemsetAsync(lb, 0, ptiles.size() * sizeof(unsigned long long) + 16, h->stream));
+    EJ_CUDA(h, cudaFuncSetAttribute(batch_write_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(PwSmem)));
+    batch_write_kernel<<<(unsigned)ptiles.size(), PR_THREADS, sizeof(PwSmem), h->stream>>>(
+        djoins, reinterpret_cast<const BatchPTile*>(A + ptiles_off), lb,
+        reinterpret_cast<unsigned int*>(lb + ptiles.size()), h->d_status);
+    EJ_TRY(ej_check_launch(h, "batch_write_kernel"));
+  }
+  ej_phase_mark(h, 4);
+  return EJ_OK;
+}
+
+static ej_status batch_check(ej_handle* h, const ej_join_desc* joins, uint32_t n) {
+  if (n && !joins) return ej_fail(h, EJ_ERR_INVALID, "joins is NULL");
+  for (uint32_t i = 0; i < n; i++) {
+    EJ_TRY(ej_check_rel(h, "R", joins[i].R, joins[i].nR));
+    EJ_TRY(ej_check_rel(h, "S", joins[i].S, joins[i].nS));
+    if (joins[i].out_cap && !joins[i].out) return ej_fail(h, EJ_ERR_INVALID, "join %u: out is NULL", i);
+    if (joins[i].out && ((uintptr_t)joins[i].out % 16))
+      return ej_fail(h, EJ_ERR_INVALID, "join %u: out must be 16-byte aligned", i);
+  }
+  return EJ_OK;
+}
+
+extern "C" ej_status ej_batch_hash_join_async(ej_handle* h, const ej_join_desc* joins, uint32_t njoins,
+                                              uint64_t* d_counts) {
+  EJ_TRY(ej_begin(h));
+  EJ_TRY(batch_check(h, joins, njoins));
+  if (njoins && !d_counts) return ej_fail(h, EJ_ERR_INVALID, "d_counts is NULL");
+  if (!njoins) return EJ_OK;
+  return batch_run(h, joins, njoins, reinterpret_cast<unsigned long long*>(d_counts));
+}
+
+extern "C" ej_status ej_batch_hash_join(ej_handle* h, const ej_join_desc* joins, uint32_t njoins, uint64_t* counts) {
+  EJ_TRY(ej_begin(h));
+  EJ_TRY(batch_check(h, joins, njoins));
+  if (njoins && !counts) return ej_fail(h, EJ_ERR_INVALID, "counts is NULL");
+  if (!njoins) return EJ_OK;
+  // device counts live in the handle's count area: grow it when needed
+  if (njoins > h->batch_counts_cap) {
+    EJ_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaFree(h->d_batch_counts);
+    cudaFreeHost(h->h_batch_counts);
+    h->d_batch_counts = nullptr;
+    h->h_batch_counts = nullptr;
+    h->batch_counts_cap = 0;
+    EJ_CUDA(h, cudaMalloc(&h->d_batch_counts, njoins * sizeof(unsigned long long)));
+    EJ_CUDA(h, cudaMallocHost(&h->h_batch_counts, njoins * sizeof(unsigned long long)));
+    h->batch_counts_cap = njoins;
+  }
+  EJ_TRY(batch_run(h, joins, njoins, h->d_batch_counts));
+  EJ_CUDA(h, cudaMemcpyAsync(h->h_batch_counts, h->d_batch_counts, njoins * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, h->stream));
+  EJ_TRY(ej_finish(h, nullptr));
+  bool over = false;
+  for (uint32_t i = 0; i < njoins; i++) {
+    counts[i] = h->h_batch_counts[i];
+    over |= counts[i] > joins[i].out_cap;
+  }
+  return over ? ej_fail(h, EJ_ERR_CAPACITY, "a join of the batch has more results than its out_cap") : EJ_OK;
+}

@@ -52,6 +52,10 @@ struct ej_handle {
   // host-buffer entry points: device staging owned separately from the arena
   void* stage = nullptr;
   size_t stage_cap = 0;
+  // synchronous batched joins: per-join counts
+  unsigned long long* d_batch_counts = nullptr;
+  unsigned long long* h_batch_counts = nullptr;
+  uint32_t batch_counts_cap = 0;
 };
 
 // Arena layout: callers first add every buffer to a plan, then reserve once.
@@ -72,8 +76,6 @@ ej_status ej_check_launch(ej_handle* h, const char* what);
 // the phase boundaries (build | partition | count | write); no-ops when timing is off
 void ej_phase_begin(ej_handle* h);
 void ej_phase_mark(ej_handle* h, int k);
-ej_status ej_read_count(ej_handle* h, uint64_t* out_count);  // sync + read d_words[0]
-ej_status ej_take_status(ej_handle* h);                      // sync + read/clear d_status
 
 #define EJ_CUDA(h, call)                                                                  \
   do {                                                                                    \
@@ -110,10 +112,22 @@ ej_status ej_scan_u64_u64(ej_handle* h, const unsigned long long* in, uint64_t n
 // key = hash32(val) (EJ_DIGIT_HASH) or the order-preserving unsigned image of
 // the signed val (EJ_DIGIT_VALUE, for sorting).
 enum { EJ_DIGIT_HASH = 0, EJ_DIGIT_VALUE = 1 };
+constexpr uint32_t EJ_RX_TILE = 4096;  // rows per radix tile
+// A tile of a segmented pass (batched joins): rows [start, start + n) of one
+// segment (n <= EJ_RX_TILE); the histogram cell of digit d is cell0 + d * stride,
+// with cells laid out segment by segment (cell0 = segment base + tile index
+// in the segment, stride = tiles of the segment), so one scan over all cells
+// keeps the segments apart in the output.
+struct ej_rx_tile {
+  unsigned long long start;
+  uint32_t n, cell0, stride, pad;
+};
+
 struct ej_radix_plan {
   uint64_t n = 0;
   uint32_t ntiles = 0;
   size_t hist_off = 0, offs_off = 0, scan_off = 0;  // arena offsets
+  const ej_rx_tile* tiles = nullptr;                // device descriptors (segmented passes)
 };
 uint32_t ej_radix_tiles(uint64_t n);
 void ej_radix_plan_add(ej_plan_bytes& p, ej_radix_plan& rp, uint64_t n);
@@ -136,11 +150,12 @@ constexpr uint64_t EJ_TABLE_PAD = 8;
 struct ej_table_view {
   int kind = EJ_TABLE_HASH;
   const int32_t* rkey = nullptr;     // [nR + pad] row ids in table order
-  const int32_t* rval = nullptr;     // [nR + pad] join keys in table order (16-byte aligned)
+  const int32_t* rval = nullptr;     // [nR + pad] join keys in table order
   const uint32_t* start = nullptr;   // [2^hb + 1] (hash)
   const int32_t* fence = nullptr;    // [nfence] (sorted)
   uint64_t nR = 0;
   uint32_t hb = 1;
   uint32_t nfence = 0;
+  uint32_t voff = 0;  // rval - voff is 16-byte aligned (tables of a batch share one array)
 };
 uint32_t ej_table_bucket_bits(uint64_t nR, int delta = 0);

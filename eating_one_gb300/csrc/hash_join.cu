@@ -31,15 +31,10 @@
 #include "ej_device.cuh"
 #include "hash_join.cuh"
 #include "probe.cuh"
+#include "probe_write.cuh"
 
 namespace {
 
-constexpr int PR_THREADS = 256;
-constexpr int PR_ITEMS = 4;
-constexpr int PR_TILE = PR_THREADS * PR_ITEMS;  // 1024 probes
-constexpr int PW_STAGE = 2048;                  // staged output rows per chunk (32 KB)
-constexpr uint32_t PW_LIGHT = 8;                // more matches: expanded by the whole block
-constexpr uint32_t NULL_RUN = 0xFFFFFFFFu;      // OUTER: the NULL-extended row
 
 // start[b] = first position of bucket b in the hash-sorted table, b in [0, 2^hb].
 __global__ void bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint32_t* __restrict__ start,
@@ -68,22 +63,19 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   __shared__ unsigned long long warp_tmp[PR_THREADS / 32 + 1];
   const uint64_t base = (uint64_t)blockIdx.x * PR_TILE;
   const int* pv = reinterpret_cast<const int*>(P) + 1;
-  int v[PR_ITEMS];
+  int32_t v[PR_ITEMS];
+  bool ok[PR_ITEMS];
 #pragma unroll
   for (int j = 0; j < PR_ITEMS; j++) {
     const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    v[j] = idx < nP ? __ldcs(pv + 2 * idx) : 0;
+    ok[j] = idx < nP;
+    v[j] = ok[j] ? __ldcs(pv + 2 * idx) : 0;
   }
+  uint32_t lo[PR_ITEMS], m[PR_ITEMS];
+  ej_find_runs<KIND, PR_ITEMS>(t, v, ok, lo, m);
   unsigned long long c = 0;
 #pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    if (idx >= nP) continue;
-    uint32_t lo, m;
-    EjRun<KIND>::find(t, v[j], lo, m);
-    if (OUTER && m == 0) m = 1;
-    c += m;
-  }
+  for (int j = 0; j < PR_ITEMS; j++) c += (OUTER && ok[j] && m[j] == 0) ? 1u : m[j];
   unsigned long long total;
   ej_block_exclusive_sum<PR_THREADS, unsigned long long>(c, warp_tmp, &total);
   if (threadIdx.x == 0) tile_count[blockIdx.x] = total;
@@ -91,25 +83,8 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
 
 // ---- write with decoupled look-back ---------------------------------------------
 
-struct PwSmem {
-  int4 stage[PW_STAGE];                   // 32 KB of output rows
-  unsigned long long pref[PR_TILE + 1];   // exclusive prefix of row counts per probe
-  int2 sprobe[PR_TILE];                   // the probe tuples
-  uint32_t run_lo[PR_TILE];               // run start (NULL_RUN: NULL-extended row)
-  uint16_t heavy[PR_TILE];                // probes expanded by the whole block
-  unsigned long long warp_tmp[PR_THREADS / 32 + 1];
-  unsigned long long tile_off;
-  unsigned int tile;
-  unsigned int nheavy;
-};
-
-__device__ __forceinline__ int4 make_row(const ej_table_view& t, uint32_t lo, uint32_t k, int2 s) {
-  if (lo == NULL_RUN) return make_int4(EJ_NULL_KEY, EJ_NULL_KEY, s.x, s.y);
-  return make_int4(__ldg(t.rkey + lo + k), s.y, s.x, s.y);
-}
-
 template <int KIND, bool OUTER>
-__global__ void __launch_bounds__(PR_THREADS)
+__global__ void __launch_bounds__(PR_THREADS, 4)
 probe_write_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* lb_status,
                    unsigned int* tile_ctr, uint64_t ntiles, ej_result* __restrict__ out, uint64_t cap,
                    unsigned long long* d_total, ej_dev_status* st) {
@@ -117,98 +92,11 @@ probe_write_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   PwSmem& sm = *reinterpret_cast<PwSmem*>(pw_smem_raw);
   if (threadIdx.x == 0) {
     sm.tile = atomicAdd(tile_ctr, 1u);  // tiles claim ids in launch order (look-back progress)
-    sm.nheavy = 0;
   }
   __syncthreads();
   const uint64_t tile = sm.tile;
-  const uint64_t base = tile * PR_TILE;
-
-  // 1. runs of the tile's probes (probe p = j * 256 + thread, in S order)
-  uint32_t cnt[PR_ITEMS];
-#pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
-    const uint32_t p = (uint32_t)j * PR_THREADS + threadIdx.x;
-    const uint64_t idx = base + p;
-    int2 s = make_int2(0, 0);
-    uint32_t lo = NULL_RUN, c = 0;
-    if (idx < nP) {
-      s = __ldcs(reinterpret_cast<const int2*>(P) + idx);
-      EjRun<KIND>::find(t, s.y, lo, c);
-      if (OUTER && c == 0) {
-        c = 1;
-        lo = NULL_RUN;
-      }
-    }
-    sm.sprobe[p] = s;
-    sm.run_lo[p] = lo;
-    sm.pref[p] = c;
-    cnt[j] = c;
-    if (c > PW_LIGHT) sm.heavy[atomicAdd(&sm.nheavy, 1u)] = (uint16_t)p;
-  }
-  __syncthreads();
-
-  // 2. exclusive prefix of the counts in probe order (4 consecutive probes per thread)
-  unsigned long long a[PR_ITEMS], local = 0;
-#pragma unroll
-  for (int e = 0; e < PR_ITEMS; e++) {
-    a[e] = sm.pref[threadIdx.x * PR_ITEMS + e];
-    local += a[e];
-  }
-  unsigned long long total;
-  unsigned long long run = ej_block_exclusive_sum<PR_THREADS, unsigned long long>(local, sm.warp_tmp, &total);
-#pragma unroll
-  for (int e = 0; e < PR_ITEMS; e++) {
-    sm.pref[threadIdx.x * PR_ITEMS + e] = run;
-    run += a[e];
-  }
-  if (threadIdx.x == 0) sm.pref[PR_TILE] = total;
-
-  // 3. the tile's output offset from its predecessors
-  if (threadIdx.x < 32) {
-    const unsigned long long off = ej_lookback_warp(lb_status, tile, total, st, 3u);
-    if (threadIdx.x == 0) sm.tile_off = off;
-  }
-  __syncthreads();
-  const unsigned long long off = sm.tile_off;
-  if (threadIdx.x == 0 && tile == ntiles - 1) {
-    *d_total = off + total;
-    if (off + total > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
-  }
-  const unsigned int nheavy = sm.nheavy;
-
-  // 4. expand runs into rows, chunk by chunk, through shared memory
-  for (unsigned long long c0 = 0; c0 < total && off + c0 < cap; c0 += PW_STAGE) {
-    const unsigned long long cend = min(total, c0 + (unsigned long long)PW_STAGE);
-#pragma unroll
-    for (int j = 0; j < PR_ITEMS; j++) {
-      const uint32_t c = cnt[j];
-      if (c == 0 || c > PW_LIGHT) continue;
-      const uint32_t p = (uint32_t)j * PR_THREADS + threadIdx.x;
-      const unsigned long long pl = sm.pref[p];
-      if (pl + c <= c0 || pl >= cend) continue;
-      const int2 s = sm.sprobe[p];
-      const uint32_t lo = sm.run_lo[p];
-      for (uint32_t k = 0; k < c; k++) {
-        const unsigned long long o = pl + k;
-        if (o >= c0 && o < cend) sm.stage[o - c0] = make_row(t, lo, k, s);
-      }
-    }
-    for (unsigned int hh = 0; hh < nheavy; hh++) {
-      const uint32_t p = sm.heavy[hh];
-      const unsigned long long pl = sm.pref[p], pe = sm.pref[p + 1];
-      const unsigned long long lo_o = max(pl, c0), hi_o = min(pe, cend);
-      const int2 s = sm.sprobe[p];
-      const uint32_t lo = sm.run_lo[p];
-      for (unsigned long long o = lo_o + threadIdx.x; o < hi_o; o += PR_THREADS)
-        sm.stage[o - c0] = make_row(t, lo, (uint32_t)(o - pl), s);
-    }
-    __syncthreads();
-    const uint32_t n = (uint32_t)(cend - c0);
-    const unsigned long long g0 = off + c0;
-    for (uint32_t i = threadIdx.x; i < n; i += PR_THREADS)
-      if (g0 + i < cap) __stcs(reinterpret_cast<int4*>(out + g0 + i), sm.stage[i]);
-    __syncthreads();
-  }
+  ej_probe_write_tile<KIND, OUTER>(sm, P, tile * PR_TILE, nP, t, lb_status, tile, tile == ntiles - 1, out, cap,
+                                   d_total, st);
 }
 
 template <int KIND, bool OUTER>

@@ -19,29 +19,86 @@ __device__ __forceinline__ uint32_t ej_bucket_of(int32_t val, uint32_t hb) {
 template <int KIND>
 struct EjRun;
 
-template <>
-struct EjRun<EJ_TABLE_HASH> {
-  static __device__ __forceinline__ void find(const ej_table_view& t, int32_t v, uint32_t& lo, uint32_t& c) {
-    const uint32_t b = ej_bucket_of(v, t.hb);
-    const uint32_t s0 = __ldg(t.start + b), s1 = __ldg(t.start + b + 1);
-    lo = s1;
-    c = 0;
+// Runs of N probe values at once, in three rounds of independent loads (bucket
+// bounds of every value, then the first 32 bytes of every bucket); only a
+// bucket longer than that continues in a loop.  ok[j] false: c[j] = 0.
+template <int N>
+__device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const int32_t (&v)[N], const bool (&ok)[N],
+                                                  uint32_t (&lo)[N], uint32_t (&c)[N]) {
+  uint32_t s0[N], s1[N];
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    s0[j] = s1[j] = 0;
+    if (ok[j]) {
+      const uint32_t b = ej_bucket_of(v[j], t.hb);
+      s0[j] = __ldg(t.start + b);
+      s1[j] = __ldg(t.start + b + 1);
+    }
+  }
+  // vector loads address the aligned base rval - voff; positions are shifted
+  // by voff while scanning and shifted back when recorded
+  const int4* rv4 = reinterpret_cast<const int4*>(t.rval - t.voff);
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    s0[j] += t.voff;
+    s1[j] += t.voff;
+  }
+  int4 qa[N], qb[N];
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    qa[j] = qb[j] = make_int4(0, 0, 0, 0);
+    const uint32_t base = s0[j] & ~3u;
+    if (s0[j] < s1[j]) {
+      qa[j] = __ldg(rv4 + base / 4);
+      if (base + 4 < s1[j]) qb[j] = __ldg(rv4 + base / 4 + 1);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    lo[j] = s1[j];
+    c[j] = 0;
     bool ended = false;
-    for (uint32_t i = s0 & ~3u; i < s1 && !ended; i += 4) {
-      const int4 q = __ldg(reinterpret_cast<const int4*>(t.rval + i));
-      const int x[4] = {q.x, q.y, q.z, q.w};
+    const uint32_t base = s0[j] & ~3u;
+    const int x[8] = {qa[j].x, qa[j].y, qa[j].z, qa[j].w, qb[j].x, qb[j].y, qb[j].z, qb[j].w};
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+      const uint32_t idx = base + (uint32_t)e;
+      if (idx < s0[j] || idx >= s1[j]) continue;
+      if (x[e] == v[j]) {
+        if (c[j] == 0) lo[j] = idx;
+        c[j]++;
+      } else if (c[j]) {
+        ended = true;  // rows are hash-sorted: the run of v is over
+      }
+    }
+    for (uint32_t i = base + 8; i < s1[j] && !ended; i += 4) {
+      const int4 q = __ldg(rv4 + i / 4);
+      const int y[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
       for (int e = 0; e < 4; e++) {
         const uint32_t idx = i + (uint32_t)e;
-        if (idx < s0 || idx >= s1) continue;
-        if (x[e] == v) {
-          if (c == 0) lo = idx;
-          c++;
-        } else if (c) {
-          ended = true;  // rows are hash-sorted: the run of v is over
+        if (idx >= s1[j]) continue;
+        if (y[e] == v[j]) {
+          if (c[j] == 0) lo[j] = idx;
+          c[j]++;
+        } else if (c[j]) {
+          ended = true;
         }
       }
     }
+    lo[j] -= t.voff;
+  }
+}
+
+template <>
+struct EjRun<EJ_TABLE_HASH> {
+  static __device__ __forceinline__ void find(const ej_table_view& t, int32_t v, uint32_t& lo, uint32_t& c) {
+    const int32_t vv[1] = {v};
+    const bool ok[1] = {true};
+    uint32_t l[1], n[1];
+    ej_find_runs_hash<1>(t, vv, ok, l, n);
+    lo = l[0];
+    c = n[0];
   }
 };
 
@@ -72,3 +129,19 @@ struct EjRun<EJ_TABLE_SORTED> {
     c = ej_fenced_bound<true>(t, v) - lo;
   }
 };
+
+// runs of N probe values (ok[j] false: c[j] = 0)
+template <int KIND, int N>
+__device__ __forceinline__ void ej_find_runs(const ej_table_view& t, const int32_t (&v)[N], const bool (&ok)[N],
+                                             uint32_t (&lo)[N], uint32_t (&c)[N]) {
+  if (KIND == EJ_TABLE_HASH) {
+    ej_find_runs_hash<N>(t, v, ok, lo, c);
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      lo[j] = 0;
+      c[j] = 0;
+      if (ok[j]) EjRun<EJ_TABLE_SORTED>::find(t, v[j], lo[j], c[j]);
+    }
+  }
+}

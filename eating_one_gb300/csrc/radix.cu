@@ -5,7 +5,7 @@
 // rpartitioning, driven by hj.cc:430-534 and :702-829): 16-thread blocks that
 // each walk 256 consecutive tuples, one 6-bit digit per pass, a host
 // round-trip per pass.  Here one pass is three launches on the stream:
-//   1. rx_hist_kernel    per 8192-tuple tile, digit counts in warp-private
+//   1. rx_hist_kernel    per 4096-tuple tile, digit counts in warp-private
 //                        shared-memory histograms, stored digit-major:
 //                        hist[digit * ntiles + tile];
 //   2. look-back scan    of the digit-major histogram gives every (digit, tile)
@@ -22,8 +22,8 @@ namespace {
 
 constexpr int RX_THREADS = 256;
 constexpr int RX_WARPS = RX_THREADS / 32;
-constexpr int RX_TILE = 8192;
-constexpr int RX_WARP_SPAN = RX_TILE / RX_WARPS;  // 1024 consecutive tuples per warp
+constexpr int RX_TILE = (int)EJ_RX_TILE;
+constexpr int RX_WARP_SPAN = RX_TILE / RX_WARPS;  // consecutive tuples per warp
 constexpr int RX_ROUNDS = RX_WARP_SPAN / 32;      // 32
 constexpr int RX_MAX_DIGITS = 256;
 
@@ -33,16 +33,43 @@ __device__ __forceinline__ uint32_t rx_digit(int32_t val, uint32_t shift, uint32
   return (key >> shift) & mask;
 }
 
+// The tile of this block: uniform EJ_RX_TILE-row tiles of one relation (tiles ==
+// nullptr; histogram cell of digit d = d * ntiles + tile), or one entry of a
+// descriptor array whose tiles never cross a segment (batched joins).
+struct RxTile {
+  uint64_t start;
+  uint32_t n, cell0, stride;
+};
+
+__device__ __forceinline__ RxTile rx_tile(const ej_rx_tile* tiles, uint64_t n, uint32_t ntiles) {
+  RxTile t;
+  if (tiles) {
+    const ej_rx_tile d = tiles[blockIdx.x];
+    t.start = d.start;
+    t.n = d.n;
+    t.cell0 = d.cell0;
+    t.stride = d.stride;
+  } else {
+    t.start = (uint64_t)blockIdx.x * RX_TILE;
+    t.n = (uint32_t)min((uint64_t)RX_TILE, n - t.start);
+    t.cell0 = blockIdx.x;
+    t.stride = ntiles;
+  }
+  return t;
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(RX_THREADS)
-rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, uint32_t* __restrict__ hist, uint32_t ntiles,
-               uint32_t shift, uint32_t mask) {
+rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __restrict__ tiles,
+               uint32_t* __restrict__ hist, uint32_t ntiles, uint32_t shift, uint32_t mask) {
   __shared__ uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];
   const uint32_t ndig = mask + 1u;
   for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&cnt[0][0])[i] = 0u;
   __syncthreads();
+  const RxTile tl = rx_tile(tiles, n, ntiles);
+  n = tl.start + tl.n;  // rows of this tile end here
   const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint64_t wbase = (uint64_t)blockIdx.x * RX_TILE + (uint64_t)warp * RX_WARP_SPAN;
+  const uint64_t wbase = tl.start + (uint64_t)warp * RX_WARP_SPAN;
   const int* vals = reinterpret_cast<const int*>(in) + 1;  // .val of tuple i at vals[2*i]
   int v[RX_ROUNDS];
 #pragma unroll
@@ -62,14 +89,14 @@ rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, uint32_t* __restrict
     uint32_t t = 0;
 #pragma unroll
     for (int w = 0; w < RX_WARPS; w++) t += cnt[w][d];
-    hist[(uint64_t)d * ntiles + blockIdx.x] = t;
+    hist[tl.cell0 + (uint64_t)d * tl.stride] = t;
   }
 }
 
 struct RxScatterSmem {
-  ej_tuple tile[RX_TILE];              // 64 KB
-  uint16_t perm[RX_TILE];              // 16 KB: sorted position -> tile index
-  uint8_t dtile[RX_TILE];              // 8 KB: digit of each tile index
+  ej_tuple tile[RX_TILE];              // 32 KB
+  uint16_t perm[RX_TILE];              // sorted position -> tile index
+  uint8_t dtile[RX_TILE];              // digit of each tile index
   uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];  // 8 KB
   uint32_t digit_start[RX_MAX_DIGITS];
   uint32_t gbase[RX_MAX_DIGITS];
@@ -80,15 +107,16 @@ struct RxScatterSmem {
 // pass of a table build) instead of tuples
 template <int KIND, bool SOA>
 __global__ void __launch_bounds__(RX_THREADS)
-rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, ej_tuple* __restrict__ out,
-                  int32_t* __restrict__ out_keys, int32_t* __restrict__ out_vals,
+rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __restrict__ tiles,
+                  ej_tuple* __restrict__ out, int32_t* __restrict__ out_keys, int32_t* __restrict__ out_vals,
                   const uint32_t* __restrict__ offs, uint32_t ntiles, uint32_t shift, uint32_t mask) {
   extern __shared__ __align__(16) unsigned char rx_smem_raw[];
   RxScatterSmem& sm = *reinterpret_cast<RxScatterSmem*>(rx_smem_raw);
   const uint32_t ndig = mask + 1u;
   const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint64_t tbase = (uint64_t)blockIdx.x * RX_TILE;
-  const uint32_t tile_n = (uint32_t)min((uint64_t)RX_TILE, n - tbase);
+  const RxTile tl = rx_tile(tiles, n, ntiles);
+  const uint64_t tbase = tl.start;
+  const uint32_t tile_n = tl.n;
 
   // 1. stage the tile (coalesced 8-byte loads, streaming: read once)
   const uint2* src = reinterpret_cast<const uint2*>(in + tbase);
@@ -127,7 +155,7 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, ej_tuple* __restr
   const uint32_t dstart = ej_block_exclusive_sum<RX_THREADS, uint32_t>(total, sm.warp_tmp, &all);
   if (threadIdx.x < ndig) {
     sm.digit_start[threadIdx.x] = dstart;
-    sm.gbase[threadIdx.x] = offs[(uint64_t)threadIdx.x * ntiles + blockIdx.x] - dstart;
+    sm.gbase[threadIdx.x] = offs[tl.cell0 + (uint64_t)threadIdx.x * tl.stride] - dstart;
   }
   __syncthreads();
 
@@ -181,16 +209,19 @@ template <int KIND, bool SOA>
 static ej_status radix_pass_kind(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
                                  int32_t* out_keys, int32_t* out_vals, uint32_t shift, uint32_t bits) {
   const uint32_t mask = (1u << bits) - 1u;
-  const uint64_t cells = (uint64_t)rp.ntiles << bits;
+  // uniform tiles use cells d * ntiles + tile; segmented tiles carry their own
+  // cells, laid out segment by segment with a stride of the segment's tiles
+  const uint64_t cells = rp.tiles ? (uint64_t)rp.ntiles * RX_MAX_DIGITS : (uint64_t)rp.ntiles << bits;
   uint32_t* hist = reinterpret_cast<uint32_t*>(ej_arena_at(h, rp.hist_off));
   uint32_t* offs = reinterpret_cast<uint32_t*>(ej_arena_at(h, rp.offs_off));
-  rx_hist_kernel<KIND><<<rp.ntiles, RX_THREADS, 0, h->stream>>>(in, rp.n, hist, rp.ntiles, shift, mask);
+  if (rp.tiles && bits != 8) return ej_fail(h, EJ_ERR_INTERNAL, "segmented radix passes use 8-bit digits");
+  rx_hist_kernel<KIND><<<rp.ntiles, RX_THREADS, 0, h->stream>>>(in, rp.n, rp.tiles, hist, rp.ntiles, shift, mask);
   EJ_TRY(ej_check_launch(h, "rx_hist_kernel"));
   EJ_TRY(ej_scan_u32_u32(h, hist, cells, offs, ej_arena_at(h, rp.scan_off)));
   EJ_CUDA(h, cudaFuncSetAttribute(rx_scatter_kernel<KIND, SOA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(RxScatterSmem)));
   rx_scatter_kernel<KIND, SOA><<<rp.ntiles, RX_THREADS, sizeof(RxScatterSmem), h->stream>>>(
-      in, rp.n, out, out_keys, out_vals, offs, rp.ntiles, shift, mask);
+      in, rp.n, rp.tiles, out, out_keys, out_vals, offs, rp.ntiles, shift, mask);
   return ej_check_launch(h, "rx_scatter_kernel");
 }
 

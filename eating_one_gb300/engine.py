@@ -165,6 +165,30 @@ class Engine:
     def sync_status(self) -> int:
         return self.lib.ej_sync_status(self.h)
 
+    def batch_hash_join(self, pairs, outs=None) -> list[torch.Tensor]:
+        """Hash-join many (R, S) pairs in one batched pipeline; returns each join's rows.
+
+        outs: optional preallocated (cap, 4) tensors; without them each output is
+        sized by its count (one count pass per join first)."""
+        self._sync_stream()
+        n = len(pairs)
+        if outs is None:
+            outs = [torch.empty((self.count("hash", R, S), 4), dtype=torch.int32, device=self.device)
+                    for R, S in pairs]
+        descs = (native.JoinDesc * max(n, 1))()
+        for i, ((R, S), o) in enumerate(zip(pairs, outs)):
+            descs[i].R, descs[i].nR = _ptr(R), R.shape[0]
+            descs[i].S, descs[i].nS = _ptr(S), S.shape[0]
+            descs[i].out, descs[i].out_cap = _ptr(o), o.shape[0]
+        counts = (C.c_uint64 * max(n, 1))()
+        self._check(self.lib.ej_batch_hash_join(self.h, descs, n, counts))
+        return [o[: counts[i]] for i, o in enumerate(outs)]
+
+    def batch_hash_join_async(self, descs, n: int, d_counts: torch.Tensor) -> None:
+        """Asynchronous batch over prepared native.JoinDesc entries; counts to d_counts (int64[n])."""
+        self._sync_stream()
+        self._check(self.lib.ej_batch_hash_join_async(self.h, descs, n, d_counts.data_ptr()))
+
     def star_join3(self, F1, F2, D1, D2, out=None) -> torch.Tensor:
         return self._run_sized(lambda o, cap, cnt: self.lib.ej_star_join3(
             self.h, _ptr(F1), _ptr(F2), F1.shape[0], _ptr(D1), D1.shape[0], _ptr(D2), D2.shape[0], o, cap, cnt),

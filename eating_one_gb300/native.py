@@ -46,6 +46,29 @@ class GenSpec(C.Structure):
     ]
 
 
+class JoinDesc(C.Structure):
+    """Mirror of ej_join_desc (include/ej.h)."""
+
+    _fields_ = [("R", C.c_void_p), ("nR", C.c_uint64), ("S", C.c_void_p), ("nS", C.c_uint64),
+                ("out", C.c_void_p), ("out_cap", C.c_uint64)]
+
+
+class ServerConfig(C.Structure):
+    """Mirror of ej_server_config (include/ej.h)."""
+
+    _fields_ = [("device", C.c_int), ("mode", C.c_int), ("lanes", C.c_uint32), ("max_batch_joins", C.c_uint32),
+                ("lane_bytes", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    """Mirror of ej_completion (include/ej.h)."""
+
+    _fields_ = [("tag", C.c_uint64), ("count", C.c_uint64), ("status", C.c_int32), ("batch_joins", C.c_uint32),
+                ("arrival_ns", C.c_uint64), ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64)]
+
+
+EJ_SERVE_BATCHED, EJ_SERVE_PER_JOIN = 0, 1
+
 _vp, _u64, _pu64, _i32 = C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_int
 
 # name -> argtypes (restype is ej_status = int unless listed in _RESTYPES)
@@ -80,6 +103,14 @@ _SIGS = {
     "ej_index_left_outer_join": [_vp, _vp, _vp, _u64, _vp, _u64, _pu64],
     "ej_star_join3": [_vp, _vp, _vp, _u64, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_join": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_batch_hash_join": [_vp, _vp, C.c_uint32, _pu64],
+    "ej_batch_hash_join_async": [_vp, _vp, C.c_uint32, _vp],
+    "ej_server_create": [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)],
+    "ej_server_submit": [_vp, C.POINTER(JoinDesc), _u64, _u64],
+    "ej_server_poll": [_vp, C.POINTER(Completion), C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32],
+    "ej_server_drain": [_vp],
+    "ej_server_destroy": [_vp],
+    "ej_now_ns": [],
     "ej_join_host": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_exclusive_scan_u32": [_vp, _vp, _u64, _vp],
     "ej_exclusive_scan_u32_noalloc": [_vp, _u64, _vp, _vp],
@@ -87,7 +118,7 @@ _SIGS = {
     "ej_checksum": [_vp, _vp, _u64, C.c_uint32, _pu64],
 }
 _RESTYPES = {"ej_status_name": C.c_char_p, "ej_last_error": C.c_char_p, "ej_scratch_bytes": C.c_uint64,
-             "ej_kernel_launches": C.c_uint64}
+             "ej_kernel_launches": C.c_uint64, "ej_now_ns": C.c_uint64}
 EJ_PHASES = 4  # build | partition | count | write
 
 _lib = None

@@ -193,6 +193,77 @@ ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tuple* F2, ui
 ej_status ej_join(ej_handle* h, ej_algo algo, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
                   uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count);
 
+/* ---- batched joins --------------------------------------------------------- */
+
+/* One hash join of a batch: device relations, device output of out_cap rows. */
+typedef struct ej_join_desc {
+  const ej_tuple* R;
+  uint64_t nR;
+  const ej_tuple* S;
+  uint64_t nS;
+  ej_result* out;
+  uint64_t out_cap;
+} ej_join_desc;
+
+/* Many hash joins as one pipeline: a fixed sequence of launches builds every
+ * join's table (segmented radix passes) and probes every join (one work queue
+ * of (join, tile) tasks), instead of one pipeline per join.  The reference runs
+ * one join per process (joins/hashJoin_gpu/main_street/hj.cc:171-1269).  Each
+ * join's rows are bitwise those of ej_single_hash_join on the same inputs.
+ * counts[i] (host) receives join i's total; EJ_ERR_CAPACITY when any join has
+ * more results than its out_cap (its rows past out_cap are dropped). */
+ej_status ej_batch_hash_join(ej_handle* h, const ej_join_desc* joins, uint32_t njoins, uint64_t* counts);
+/* Asynchronous form: counts go to the device array d_counts[njoins]; no host
+ * synchronisation (the join descriptors are copied before the call returns). */
+ej_status ej_batch_hash_join_async(ej_handle* h, const ej_join_desc* joins, uint32_t njoins, uint64_t* d_counts);
+
+/* ---- serving: continuous batching of join requests -------------------------- */
+
+/* A request server on one device.  Requests (device relations and a device
+ * output of out_cap rows, owned by the client until the request completes)
+ * queue on submission; whenever one of the server's lanes is free, its
+ * scheduler thread takes the queued requests in arrival order, up to
+ * max_batch_joins and up to the lane's device-scratch budget (the request's
+ * footprint: its R copies and table plus the probe work queue), and launches
+ * them as one batch (EJ_SERVE_BATCHED, ej_batch_hash_join_async) or each as
+ * its own pipeline (EJ_SERVE_PER_JOIN, ej_hash_join_async).  Lanes run on
+ * their own streams, so batches overlap on the device; each lane keeps its
+ * scratch arena across batches.  The reference has no server (one join per
+ * process). */
+typedef enum ej_serve_mode { EJ_SERVE_BATCHED = 0, EJ_SERVE_PER_JOIN = 1 } ej_serve_mode;
+
+typedef struct ej_server_config {
+  int device;
+  int mode;                 /* ej_serve_mode */
+  uint32_t lanes;           /* batches in flight at once (0: 2) */
+  uint32_t max_batch_joins; /* joins per batch (0: 1024); 1 in EJ_SERVE_PER_JOIN */
+  uint64_t lane_bytes;      /* device scratch budget per lane (0: 16 GiB); a single
+                               larger request still runs, alone */
+} ej_server_config;
+
+typedef struct ej_completion {
+  uint64_t tag;          /* the submit tag */
+  uint64_t count;        /* the join's result count (rows past out_cap dropped) */
+  int32_t status;        /* EJ_OK, EJ_ERR_CAPACITY or the batch's error */
+  uint32_t batch_joins;  /* joins in the batch that carried the request */
+  uint64_t arrival_ns;   /* ej_now_ns() clock: arrival, launch, completion */
+  uint64_t launch_ns;
+  uint64_t done_ns;
+} ej_completion;
+
+typedef struct ej_server ej_server;
+
+ej_status ej_server_create(const ej_server_config* cfg, ej_server** out);
+/* Queue one request (thread-safe).  arrival_ns = 0 stamps the current time. */
+ej_status ej_server_submit(ej_server* s, const ej_join_desc* join, uint64_t tag, uint64_t arrival_ns);
+/* Take up to max completions; waits up to wait_us microseconds for the first. */
+ej_status ej_server_poll(ej_server* s, ej_completion* out, uint32_t max, uint32_t* n, uint32_t wait_us);
+/* Wait until every submitted request has completed (its completion can still be polled). */
+ej_status ej_server_drain(ej_server* s);
+ej_status ej_server_destroy(ej_server* s);
+/* monotonic clock of the server, nanoseconds */
+uint64_t ej_now_ns(void);
+
 /* ---- host-buffer entry points --------------------------------------------- */
 
 /* Same as ej_join, but R, S and out are HOST buffers (pinned memory is fastest):
