@@ -127,6 +127,18 @@ def aggregate(per_rank_ms: list[float], units_per_rank: float, steps: int) -> tu
     return units_per_rank * len(per_rank_ms) * steps / (ms * steps / 1000.0), ms
 
 
+def gather_ms(ms: float, dist, device) -> list[float]:
+    """Every rank's ms per step (all_gather; works on nccl with a CUDA device
+    and on gloo with the CPU).  Single process: [ms]."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return [ms]
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    g = [torch.zeros_like(t) for _ in range(dist.get_world_size())]
+    dist.all_gather(g, t)
+    return [float(x.item()) for x in g]
+
+
 def cpu_baseline_sample(scale: int = 4) -> dict:
     """The oracle's hash_cpu restatement on a 1/2^scale-size sample of every
     variant (generation excluded, as the reference times it), one thread each."""
@@ -264,6 +276,95 @@ def run_serve(n_requests: int, n_instances: int, lanes: int) -> None:
     del torch
 
 
+def run_configs(steps: int) -> None:
+    """The other configurations, each timed with CUDA events over `steps`
+    device-resident runs after warm-up; one JSON line per configuration."""
+    import torch
+
+    from eating_one_gb300.build import build
+    from eating_one_gb300.engine import Engine
+    from eating_one_gb300.workloads import workload
+
+    build()
+    eng = Engine(0)
+    peaks = load_peaks()
+    props = torch.cuda.get_device_properties(0)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, n=steps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    def hbm(alg, ms):
+        gbs = alg / (ms / 1000.0) / 1e9
+        return {"alg_bytes": int(alg), "achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4),
+                "peak_source": peaks["source"]}
+
+    lines = []
+    # C1: the parity configuration at full size
+    w = workload("c1")
+    R, S = eng.generate(w["R"]), eng.generate(w["S"])
+    n = eng.count("hash", R, S)
+    out = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    ms = timed(lambda: eng.hash_join(R, S, out=out))
+    lines.append({"config": "C1 hash join R=2^20 unique x S=2^22", "ms": round(ms, 4), "rows": n,
+                  "tuples_per_s": (R.shape[0] + S.shape[0]) / (ms / 1000),
+                  "roofline": hbm(24 * (R.shape[0] + S.shape[0]) + 16 * n, ms)})
+    # C2: block nested loop, all 2^36 pairs
+    w = workload("c2")
+    R, S = eng.generate(w["R"]), eng.generate(w["S"])
+    n = eng.count("bnl", R, S)
+    out = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    ms = timed(lambda: eng.join("bnl", R, S, out=out), max(3, steps // 4))
+    pairs = R.shape[0] * S.shape[0]
+    issue = props.multi_processor_count * 128 * 2.07e9  # one INT32 lane-instruction per clock per lane
+    lines.append({"config": "C2 BNLJ R=2^16 x S=2^20, keys uniform in [0, 2^16)", "ms": round(ms, 4), "rows": n,
+                  "pair_compares_per_s": pairs / (ms / 1000),
+                  "roofline": {"bound": "int32 issue", "peak_lane_ops_per_s": issue,
+                               "frac_at_one_op_per_compare": round(pairs / (ms / 1000) / issue, 4)},
+                  "reference_gpu_log": "2^20 x 2^16 in 1.483 s (nestLoopJoin, sm_35)"})
+    # C4: index joins, outer join, star join
+    w = workload("c4")
+    R, S = eng.generate(w["R"]), eng.generate(w["S"])
+    for kind in ("hash", "sort"):
+        t_build = timed(lambda: eng.build_index(kind, R).free(), 3)
+        ix = eng.build_index(kind, R)
+        n = ix.count(S)
+        out = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+        ms = timed(lambda: ix.join(S, out=out))
+        lines.append({"config": "C4 %s-index join R=2^24 x S=2^26 (50%% match)" % kind, "probe_ms": round(ms, 4),
+                      "build_ms": round(t_build, 4), "rows": n,
+                      "tuples_per_s": (R.shape[0] + S.shape[0]) / ((ms + t_build) / 1000),
+                      "roofline": hbm(16 * R.shape[0] + 8 * S.shape[0] + 16 * n, ms + t_build)})
+        ix.free()
+    n = eng.count("left_outer", R, S)
+    out = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    ms = timed(lambda: eng.join("left_outer", R, S, out=out))
+    lines.append({"config": "C4 left outer join R=2^24 x S=2^26", "ms": round(ms, 4), "rows": n,
+                  "tuples_per_s": (R.shape[0] + S.shape[0]) / (ms / 1000),
+                  "roofline": hbm(24 * (R.shape[0] + S.shape[0]) + 16 * n, ms)})
+    w = workload("c4_star")
+    t = {k: eng.generate(v) for k, v in w.items()}
+    args = (t["F1"], t["F2"], t["D1"], t["D2"])
+    n = eng.star_join3(*args).shape[0]
+    out = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+    ms = timed(lambda: eng.star_join3(*args, out=out))
+    nd = t["D1"].shape[0] + t["D2"].shape[0]
+    lines.append({"config": "C4 star join F=2^26 x D1, D2 = 2^20", "ms": round(ms, 4), "rows": n,
+                  "tuples_per_s": (2 * t["F1"].shape[0] + nd) / (ms / 1000),
+                  "roofline": hbm(8 * nd + 16 * t["F1"].shape[0] + 32 * n, ms)})
+    for ln in lines:
+        print(json.dumps(ln), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -279,8 +380,12 @@ def main() -> None:
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--lanes", type=int, default=2)
+    ap.add_argument("--configs", action="store_true", help="time configurations C1, C2 and C4 instead")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.configs:
+        run_configs(args.steps if args.steps != 30 else 10)
+        return
     if args.serve:
         run_serve(args.requests, args.instances, args.lanes)
         return
@@ -362,12 +467,7 @@ def main() -> None:
         assert int(j["d_count"].item()) == j["n_out"], (j["name"], int(j["d_count"].item()), j["n_out"])
     assert status == 0, "device status %d: %s" % (status, eng.last_error())
 
-    per_rank = [ms]
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        g = [torch.zeros_like(t) for _ in range(world)]
-        dist.all_gather(g, t)
-        per_rank = [float(x.item()) for x in g]
+    per_rank = gather_ms(ms, dist, torch.device("cuda", local))
     value, ms_max = aggregate(per_rank, units, 1)
 
     # roofline of the dominant phase (per join, averaged over the timed joins)

@@ -3,6 +3,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -173,9 +174,44 @@ extern "C" ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value) {
     case EJ_OPT_BUCKET_BITS_DELTA:
       if (value < -3 || value > 3) return ej_fail(h, EJ_ERR_INVALID, "bucket bits delta must be -3..3");
       h->opt_bucket_delta = (int)value;
+      h->opt_bucket_delta_set = value != 0;  // 0 hands the choice back to the tuning table
       return EJ_OK;
   }
   return ej_fail(h, EJ_ERR_INVALID, "unknown option %d", (int)opt);
+}
+
+extern "C" ej_status ej_set_tuning(ej_handle* h, const ej_tune_entry* entries, uint32_t n) {
+  if (!h || (n && !entries)) return EJ_ERR_INVALID;
+  std::vector<ej_tune_entry> t(entries, entries + n);
+  for (const ej_tune_entry& e : t) {
+    if (e.log2_rows > 32 || e.partition_bits < -1 || e.partition_bits > 8 || e.bucket_delta < -3 ||
+        e.bucket_delta > 3)
+      return ej_fail(h, EJ_ERR_INVALID, "bad tuning entry (log2_rows %u)", e.log2_rows);
+  }
+  std::sort(t.begin(), t.end(),
+            [](const ej_tune_entry& a, const ej_tune_entry& b) { return a.log2_rows < b.log2_rows; });
+  h->tuning = t;
+  return EJ_OK;
+}
+
+static const ej_tune_entry* tuning_for(const ej_handle* h, uint64_t nR) {
+  const ej_tune_entry* best = nullptr;
+  const uint32_t lg = ej_ceil_log2(nR < 1 ? 1 : nR);
+  for (const ej_tune_entry& e : h->tuning)
+    if (e.log2_rows <= lg) best = &e;
+  return best;
+}
+
+int ej_tuned_bucket_delta(const ej_handle* h, uint64_t nR) {
+  if (h->opt_bucket_delta_set) return h->opt_bucket_delta;
+  const ej_tune_entry* e = tuning_for(h, nR);
+  return e ? e->bucket_delta : 0;
+}
+
+int ej_tuned_partition_bits(const ej_handle* h, uint64_t nR) {
+  if (h->opt_partition_bits >= 0) return h->opt_partition_bits;
+  const ej_tune_entry* e = tuning_for(h, nR);
+  return e ? e->partition_bits : -1;
 }
 
 extern "C" ej_status ej_last_phase_ms(ej_handle* h, float ms[EJ_PHASES]) {
@@ -331,14 +367,31 @@ extern "C" ej_status ej_join(ej_handle* h, ej_algo algo, const ej_tuple* R, uint
 
 // ---- host-buffer path ------------------------------------------------------------
 
+// A device address for a host buffer the GPU can store to directly: pinned
+// (page-locked, mapped) host memory.  nullptr for pageable memory, which is
+// staged through device memory instead.
+static void* mapped_view(void* host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
 extern "C" ej_status ej_join_host(ej_handle* h, ej_algo algo, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
                                   uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count) {
   EJ_TRY(ej_begin(h));
   if ((nR && !R) || (nS && !S) || (out_cap && !out) || !out_count) return ej_fail(h, EJ_ERR_INVALID, "null buffer");
+  // pinned output: the write pass stores rows straight into host memory over
+  // the CPU-GPU link, so no device copy of the output and no download pass
+  ej_result* direct = out_cap ? static_cast<ej_result*>(mapped_view(out)) : nullptr;
+  if (direct && !aligned(direct, 16)) direct = nullptr;
   ej_plan_bytes p;
   const size_t r_off = p.add(nR * sizeof(ej_tuple));
   const size_t s_off = p.add(nS * sizeof(ej_tuple));
-  const size_t o_off = p.add(out_cap * sizeof(ej_result));
+  const size_t o_off = p.add(direct ? 0 : out_cap * sizeof(ej_result));
   if (p.bytes > h->stage_cap) {
     EJ_CUDA(h, cudaStreamSynchronize(h->stream));
     if (h->stage) EJ_CUDA(h, cudaFree(h->stage));
@@ -353,7 +406,7 @@ extern "C" ej_status ej_join_host(ej_handle* h, ej_algo algo, const ej_tuple* R,
   char* base = static_cast<char*>(h->stage);
   ej_tuple* dR = reinterpret_cast<ej_tuple*>(base + r_off);
   ej_tuple* dS = reinterpret_cast<ej_tuple*>(base + s_off);
-  ej_result* dO = reinterpret_cast<ej_result*>(base + o_off);
+  ej_result* dO = direct ? direct : reinterpret_cast<ej_result*>(base + o_off);
   if (nR) EJ_CUDA(h, cudaMemcpyAsync(dR, R, nR * sizeof(ej_tuple), cudaMemcpyHostToDevice, h->stream));
   if (nS) EJ_CUDA(h, cudaMemcpyAsync(dS, S, nS * sizeof(ej_tuple), cudaMemcpyHostToDevice, h->stream));
   uint64_t count = 0;
@@ -361,7 +414,7 @@ extern "C" ej_status ej_join_host(ej_handle* h, ej_algo algo, const ej_tuple* R,
   *out_count = count;
   if (st != EJ_OK && st != EJ_ERR_CAPACITY) return st;
   const uint64_t rows = count < out_cap ? count : out_cap;
-  if (rows) {
+  if (rows && !direct) {
     EJ_CUDA(h, cudaMemcpyAsync(out, dO, rows * sizeof(ej_result), cudaMemcpyDeviceToHost, h->stream));
     EJ_CUDA(h, cudaStreamSynchronize(h->stream));
   }

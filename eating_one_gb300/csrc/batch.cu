@@ -112,7 +112,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     b.r_row0 = nr_total;
     b.view.kind = EJ_TABLE_HASH;
     b.view.nR = nR;
-    b.view.hb = ej_table_bucket_bits(nR, h->opt_bucket_delta);
+    b.view.hb = ej_table_bucket_bits(nR, ej_tuned_bucket_delta(h, nR));
     const uint32_t rt = (uint32_t)((nR + BX_RX_TILE - 1) / BX_RX_TILE);
     for (uint32_t t = 0; t < rt; t++) {
       ej_rx_tile d;

@@ -46,9 +46,11 @@ struct ej_handle {
   int last_set = -1;          // last fully recorded set
   unsigned long long launches = 0;  // kernels launched through ej_check_launch
   ej_zipf_cache zipf;
-  // tuning overrides (-1 / 0 = planner's choice)
+  // tuning overrides (-1 / 0 = planner's choice) and the autotuned table
   int opt_partition_bits = -1;
   int opt_bucket_delta = 0;
+  bool opt_bucket_delta_set = false;
+  std::vector<ej_tune_entry> tuning;  // ascending log2_rows
   // host-buffer entry points: device staging owned separately from the arena
   void* stage = nullptr;
   size_t stage_cap = 0;
@@ -159,3 +161,7 @@ struct ej_table_view {
   uint32_t voff = 0;  // rval - voff is 16-byte aligned (tables of a batch share one array)
 };
 uint32_t ej_table_bucket_bits(uint64_t nR, int delta = 0);
+// the bucket-bits delta and the S partition bits (-1: planner) that apply to a
+// build side of nR rows: explicit options first, then the tuning table
+int ej_tuned_bucket_delta(const ej_handle* h, uint64_t nR);
+int ej_tuned_partition_bits(const ej_handle* h, uint64_t nR);

@@ -252,9 +252,10 @@ ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
 
 uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS) {
   (void)nS;
-  const uint32_t hb = ej_table_bucket_bits(nR, h->opt_bucket_delta);
-  if (h->opt_partition_bits >= 0) return std::min<uint32_t>((uint32_t)h->opt_partition_bits, std::min(hb, 8u));
-  const double table = (double)ej_table_bytes(nR, h->opt_bucket_delta);
+  const uint32_t hb = ej_table_bucket_bits(nR, ej_tuned_bucket_delta(h, nR));
+  const int forced = ej_tuned_partition_bits(h, nR);
+  if (forced >= 0) return std::min<uint32_t>((uint32_t)forced, std::min(hb, 8u));
+  const double table = (double)ej_table_bytes(nR, ej_tuned_bucket_delta(h, nR));
   const double l2 = (double)(h->l2_bytes ? h->l2_bytes : (size_t)126 << 20);
   if (table <= l2 / 4.0) return 0;  // the whole table stays L2-resident
   // one partition's table region should be a few MB so that the partitions in
@@ -308,7 +309,7 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   const uint32_t pb = (mode == 1) ? 0u : ej_probe_partition_bits(h, nR, nS);
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, h->opt_bucket_delta);
+  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR));
   ej_probe_layout L;
   ej_probe_layout_add(p, L, nS, pb);
   EJ_TRY(ej_arena_reserve(h, p.bytes));

@@ -41,7 +41,7 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
   *out = nullptr;
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/true, kind, h->opt_bucket_delta);
+  ej_table_plan(p, tp, nR, /*own_storage=*/true, kind, ej_tuned_bucket_delta(h, nR));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_index* ix = new ej_index();
   ix->kind = kind;
@@ -158,7 +158,7 @@ extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_
   const uint32_t pb = ej_probe_partition_bits(h, nR, nS);
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, h->opt_bucket_delta);
+  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR));
   ej_probe_layout L;
   ej_probe_layout_add(p, L, nS, pb);
   EJ_TRY(ej_arena_reserve(h, p.bytes));

@@ -67,6 +67,13 @@ class Completion(C.Structure):
                 ("arrival_ns", C.c_uint64), ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64)]
 
 
+class TuneEntry(C.Structure):
+    """Mirror of ej_tune_entry (include/ej.h)."""
+
+    _fields_ = [("log2_rows", C.c_uint32), ("partition_bits", C.c_int32), ("bucket_delta", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 EJ_SERVE_BATCHED, EJ_SERVE_PER_JOIN = 0, 1
 
 _vp, _u64, _pu64, _i32 = C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_int
@@ -85,6 +92,7 @@ _SIGS = {
     "ej_phase_totals": [_vp, C.POINTER(C.c_double), C.POINTER(C.c_uint32)],
     "ej_kernel_launches": [_vp],
     "ej_set_option": [_vp, _i32, C.c_int64],
+    "ej_set_tuning": [_vp, _vp, C.c_uint32],
     "ej_hash_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_hash_join_count": [_vp, _vp, _u64, _vp, _u64, _pu64],
     "ej_hash_join_async": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _vp],

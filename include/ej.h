@@ -117,6 +117,19 @@ typedef enum ej_option {
 } ej_option;
 ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value);
 
+/* A tuning table (written by the autotuner, eating_one_gb300/autotune.py):
+ * for joins whose build side has at least 2^log2_rows rows (the entry with the
+ * largest such log2_rows applies), the S partition bits (-1: planner) and the
+ * bucket-bits delta.  Options set with ej_set_option take precedence.
+ * n = 0 clears the table. */
+typedef struct ej_tune_entry {
+  uint32_t log2_rows;
+  int32_t partition_bits;
+  int32_t bucket_delta;
+  int32_t reserved;
+} ej_tune_entry;
+ej_status ej_set_tuning(ej_handle* h, const ej_tune_entry* entries, uint32_t n);
+
 /* ---- equi-joins on device relations ------------------------------------- */
 
 /* Radix-partitioned hash join (replaces join() of joins/hashJoin_gpu/main_street/hj.cc:171-1269:
