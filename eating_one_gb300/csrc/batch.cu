@@ -74,14 +74,12 @@ __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, 
   }
 }
 
-__global__ void __launch_bounds__(PR_THREADS, 4)
+__global__ void __launch_bounds__(PR_THREADS, 3)
 batch_write_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
                    unsigned long long* lb_status, unsigned int* tile_ctr, ej_dev_status* st) {
-  extern __shared__ __align__(16) unsigned char bw_smem_raw[];
-  PwSmem& sm = *reinterpret_cast<PwSmem*>(bw_smem_raw);
-  if (threadIdx.x == 0) {
-    sm.tile = atomicAdd(tile_ctr, 1u);  // global work queue, join by join
-  }
+  extern __shared__ __align__(16) unsigned char pw_smem_raw[];
+  PwSmem& sm = *reinterpret_cast<PwSmem*>(pw_smem_raw);
+  if (threadIdx.x == 0) sm.tile = atomicAdd(tile_ctr, 1u);  // global work queue, join by join
   __syncthreads();
   const BatchPTile pt = ptiles[sm.tile];
   const BatchJoin& j = joins[pt.join];

@@ -119,18 +119,25 @@ __device__ __forceinline__ T ej_block_exclusive_sum(T v, T* warp_tmp, T* total) 
 #define EJ_LB_PREFIX 2ull
 #define EJ_LB_VALUE_MASK ((1ull << 62) - 1ull)
 
-// Called by one full warp.  Publishes `aggregate` for `tile`, looks back over
-// the predecessors and publishes the inclusive prefix.  Returns the exclusive
-// prefix of the tile (in every lane).
-__device__ __forceinline__ unsigned long long ej_lookback_warp(unsigned long long* status, uint64_t tile,
-                                                             unsigned long long aggregate,
-                                                             ej_dev_status* st, unsigned int where) {
+// Both halves are called by one full warp; the exclusive prefix is returned
+// in every lane.  The two halves of a look-back step, so that a tile can do
+// other work between them: publish the tile's aggregate (tile 0: its
+// inclusive prefix)...
+__device__ __forceinline__ void ej_lookback_publish(unsigned long long* status, uint64_t tile,
+                                                    unsigned long long aggregate) {
+  if ((threadIdx.x & 31u) == 0)
+    ej_st_relaxed(&status[tile], ((tile == 0 ? EJ_LB_PREFIX : EJ_LB_AGG) << 62) | (aggregate & EJ_LB_VALUE_MASK));
+}
+
+// ...then walk back over the predecessors (32 per step, one per lane) until
+// one with an inclusive prefix, publish this tile's inclusive prefix and
+// return its exclusive one.  A wait longer than EJ_WAIT_LIMIT_NS takes the
+// missing predecessors as zero and records EJ_ERR_TIMEOUT at `where`.
+__device__ __forceinline__ unsigned long long ej_lookback_resolve(unsigned long long* status, uint64_t tile,
+                                                                  unsigned long long aggregate,
+                                                                  ej_dev_status* st, unsigned int where) {
   const unsigned int lane = threadIdx.x & 31u;
-  if (tile == 0) {
-    if (lane == 0) ej_st_relaxed(&status[0], (EJ_LB_PREFIX << 62) | (aggregate & EJ_LB_VALUE_MASK));
-    return 0ull;
-  }
-  if (lane == 0) ej_st_relaxed(&status[tile], (EJ_LB_AGG << 62) | (aggregate & EJ_LB_VALUE_MASK));
+  if (tile == 0) return 0ull;
   unsigned long long exclusive = 0;
   int64_t k = (int64_t)tile - 1;
   const unsigned long long t0 = ej_globaltimer();
@@ -167,4 +174,12 @@ __device__ __forceinline__ unsigned long long ej_lookback_warp(unsigned long lon
     if (gave_up) ej_set_status(st, EJ_ERR_TIMEOUT, where);
   }
   return exclusive;
+}
+
+// both halves at once
+__device__ __forceinline__ unsigned long long ej_lookback_warp(unsigned long long* status, uint64_t tile,
+                                                             unsigned long long aggregate,
+                                                             ej_dev_status* st, unsigned int where) {
+  ej_lookback_publish(status, tile, aggregate);
+  return ej_lookback_resolve(status, tile, aggregate, st, where);
 }

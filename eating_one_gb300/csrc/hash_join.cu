@@ -22,9 +22,8 @@
 //          its counts, takes its output offset from the preceding tiles by
 //          decoupled look-back (tiles claim ids in order), then expands the
 //          runs into rows staged in shared memory and written out as
-//          coalesced 16-byte streaming stores.  Probes with many matches are
-//          expanded by the whole block.  The separate count kernel + scan
-//          serve the *_count entry points.  Output order is deterministic:
+//          coalesced 16-byte streaming stores (probe_write.cuh).  The
+//          separate count kernel + scan serve the *_count entry points.  Output order is deterministic:
 //          tile, probe, then R run order.
 // The same kernels serve the sort index (runs by binary search) and the left
 // outer join (OUTER: a probe without matches yields one NULL-extended row).
@@ -55,44 +54,28 @@ __global__ void fence_kernel(const int32_t* __restrict__ rval, int32_t* __restri
 }
 
 // ---- count (for the *_count entry points) ---------------------------------------
+// Each warp tile's row total; a scan of the totals gives the join's size.
 
 template <int KIND, bool OUTER>
 __global__ void __launch_bounds__(PR_THREADS)
-probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
-                   unsigned long long* __restrict__ tile_count) {
-  __shared__ unsigned long long warp_tmp[PR_THREADS / 32 + 1];
-  const uint64_t base = (uint64_t)blockIdx.x * PR_TILE;
-  const int* pv = reinterpret_cast<const int*>(P) + 1;
-  int32_t v[PR_ITEMS];
-  bool ok[PR_ITEMS];
-#pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * PR_THREADS + threadIdx.x;
-    ok[j] = idx < nP;
-    v[j] = ok[j] ? __ldcs(pv + 2 * idx) : 0;
-  }
-  uint32_t lo[PR_ITEMS], m[PR_ITEMS];
-  ej_find_runs<KIND, PR_ITEMS>(t, v, ok, lo, m);
-  unsigned long long c = 0;
-#pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) c += (OUTER && ok[j] && m[j] == 0) ? 1u : m[j];
-  unsigned long long total;
-  ej_block_exclusive_sum<PR_THREADS, unsigned long long>(c, warp_tmp, &total);
-  if (threadIdx.x == 0) tile_count[blockIdx.x] = total;
+probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* __restrict__ wcount,
+                   uint64_t nwtiles) {
+  const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + (threadIdx.x >> 5);
+  if (w >= nwtiles) return;
+  const unsigned long long total = ej_probe_count_warp<KIND, OUTER>(P, w * PR_WTILE, nP, t);
+  if ((threadIdx.x & 31u) == 0) wcount[w] = total;
 }
 
 // ---- write with decoupled look-back ---------------------------------------------
 
 template <int KIND, bool OUTER>
-__global__ void __launch_bounds__(PR_THREADS, 4)
+__global__ void __launch_bounds__(PR_THREADS, 3)
 probe_write_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* lb_status,
                    unsigned int* tile_ctr, uint64_t ntiles, ej_result* __restrict__ out, uint64_t cap,
                    unsigned long long* d_total, ej_dev_status* st) {
   extern __shared__ __align__(16) unsigned char pw_smem_raw[];
   PwSmem& sm = *reinterpret_cast<PwSmem*>(pw_smem_raw);
-  if (threadIdx.x == 0) {
-    sm.tile = atomicAdd(tile_ctr, 1u);  // tiles claim ids in launch order (look-back progress)
-  }
+  if (threadIdx.x == 0) sm.tile = atomicAdd(tile_ctr, 1u);  // tiles claim ids in launch order (look-back progress)
   __syncthreads();
   const uint64_t tile = sm.tile;
   ej_probe_write_tile<KIND, OUTER>(sm, P, tile * PR_TILE, nP, t, lb_status, tile, tile == ntiles - 1, out, cap,
@@ -101,8 +84,8 @@ probe_write_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
 
 template <int KIND, bool OUTER>
 ej_status launch_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                       unsigned long long* tcount) {
-  probe_count_kernel<KIND, OUTER><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, tcount);
+                       unsigned long long* wcount) {
+  probe_count_kernel<KIND, OUTER><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles);
   return ej_check_launch(h, "probe_count_kernel");
 }
 
@@ -210,27 +193,28 @@ uint64_t ej_probe_tiles(uint64_t nP) { return (nP + PR_TILE - 1) / PR_TILE; }
 void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP) {
   pp.nP = nP;
   pp.ntiles = ej_probe_tiles(nP);
-  pp.count_off = p.add((pp.ntiles + 1) * sizeof(unsigned long long));
-  pp.off_off = p.add((pp.ntiles + 1) * sizeof(unsigned long long));
-  pp.scan_off = p.add(ej_scan_scratch_bytes(pp.ntiles));
+  pp.nwtiles = (nP + PR_WTILE - 1) / PR_WTILE;
+  pp.count_off = p.add((pp.nwtiles + 1) * sizeof(unsigned long long));
+  pp.off_off = p.add((pp.nwtiles + 1) * sizeof(unsigned long long));
+  pp.scan_off = p.add(ej_scan_scratch_bytes(pp.nwtiles));
   pp.lb_off = p.add(pp.ntiles * sizeof(unsigned long long) + 16);
 }
 
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                          bool outer, unsigned long long* d_count) {
-  unsigned long long* tcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.count_off));
-  unsigned long long* toff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.off_off));
+  unsigned long long* wcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.count_off));
+  unsigned long long* woff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.off_off));
   if (pp.ntiles) {
     if (t.kind == EJ_TABLE_HASH)
-      EJ_TRY(outer ? launch_count<EJ_TABLE_HASH, true>(h, pp, P, t, tcount)
-                   : launch_count<EJ_TABLE_HASH, false>(h, pp, P, t, tcount));
+      EJ_TRY(outer ? launch_count<EJ_TABLE_HASH, true>(h, pp, P, t, wcount)
+                   : launch_count<EJ_TABLE_HASH, false>(h, pp, P, t, wcount));
     else
-      EJ_TRY(outer ? launch_count<EJ_TABLE_SORTED, true>(h, pp, P, t, tcount)
-                   : launch_count<EJ_TABLE_SORTED, false>(h, pp, P, t, tcount));
+      EJ_TRY(outer ? launch_count<EJ_TABLE_SORTED, true>(h, pp, P, t, wcount)
+                   : launch_count<EJ_TABLE_SORTED, false>(h, pp, P, t, wcount));
   }
-  EJ_TRY(ej_scan_u64_u64(h, tcount, pp.ntiles, toff, ej_arena_at(h, pp.scan_off)));
+  EJ_TRY(ej_scan_u64_u64(h, wcount, pp.nwtiles, woff, ej_arena_at(h, pp.scan_off)));
   if (d_count)
-    EJ_CUDA(h, cudaMemcpyAsync(d_count, toff + pp.ntiles, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+    EJ_CUDA(h, cudaMemcpyAsync(d_count, woff + pp.nwtiles, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
                                h->stream));
   return EJ_OK;
 }

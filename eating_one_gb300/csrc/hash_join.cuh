@@ -20,7 +20,8 @@ struct ej_table_plan_t {
 
 struct ej_probe_plan_t {
   uint64_t nP = 0;
-  uint64_t ntiles = 0;
+  uint64_t ntiles = 0;   // blocks of 1024 probes
+  uint64_t nwtiles = 0;  // warp tiles of 128 probes
   size_t count_off = 0, off_off = 0, scan_off = 0, lb_off = 0;
 };
 
@@ -42,10 +43,11 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
 
 uint64_t ej_probe_tiles(uint64_t nP);
 void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP);
-// count kernel + scan; the total goes to *d_count (device) when d_count != nullptr
+// count pass + scan of the warp-tile totals; the total goes to *d_count (device)
+// when d_count != nullptr
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                          bool outer, unsigned long long* d_count);
-// write kernel with look-back tile offsets; the total goes to *d_count
+// write pass with decoupled look-back; the total goes to *d_count (device)
 ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                          bool outer, ej_result* out, uint64_t cap, unsigned long long* d_count);
 

@@ -55,22 +55,21 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
   }
 #pragma unroll
   for (int j = 0; j < N; j++) {
-    lo[j] = s1[j];
-    c[j] = 0;
-    bool ended = false;
+    // equality mask of the 8 loaded values, restricted to the bucket
     const uint32_t base = s0[j] & ~3u;
     const int x[8] = {qa[j].x, qa[j].y, qa[j].z, qa[j].w, qb[j].x, qb[j].y, qb[j].z, qb[j].w};
+    uint32_t eq = 0;
 #pragma unroll
-    for (int e = 0; e < 8; e++) {
-      const uint32_t idx = base + (uint32_t)e;
-      if (idx < s0[j] || idx >= s1[j]) continue;
-      if (x[e] == v[j]) {
-        if (c[j] == 0) lo[j] = idx;
-        c[j]++;
-      } else if (c[j]) {
-        ended = true;  // rows are hash-sorted: the run of v is over
-      }
-    }
+    for (int e = 0; e < 8; e++) eq |= (x[e] == v[j] ? 1u : 0u) << e;
+    const uint32_t from = s0[j] - base;                            // 0..3
+    const uint32_t to = s1[j] - base < 8u ? s1[j] - base : 8u;     // end of the bucket within the 8
+    eq &= ((1u << to) - 1u) & ~((1u << from) - 1u);
+    // rows are hash-sorted, so the matches are one contiguous run
+    c[j] = __popc(eq);
+    lo[j] = c[j] ? base + (uint32_t)(__ffs(eq) - 1) : s1[j];
+    // a run goes on past the 8 loaded values only if it reaches their end; with
+    // no match yet, the search goes on only if the bucket does
+    bool ended = c[j] ? !(eq & 0x80u) : (to < 8u);
     for (uint32_t i = base + 8; i < s1[j] && !ended; i += 4) {
       const int4 q = __ldg(rv4 + i / 4);
       const int y[4] = {q.x, q.y, q.z, q.w};

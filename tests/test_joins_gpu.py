@@ -55,6 +55,7 @@ CASES = [  # (nR, nS, key range) - unique-ish, many-to-many, heavy duplicates, r
     (65536, 65536, (INT_MIN, INT_MAX)),
     (12345, 54321, (-1000, 1000)),
     (1, 1, (7, 8)),
+    (2000, 3000, (0, 8)),  # ~250 rows per probe: groups larger than the write buffer
 ]
 
 
