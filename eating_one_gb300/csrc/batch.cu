@@ -10,10 +10,12 @@
 //               the digit histograms are laid out join by join, so one scan
 //               places every join's rows in its own range, hash-sorted
 //   starts      every join's bucket starts in one launch (its own bucket bits)
-//   write       one launch over every join's probe tiles: a tile claims the
-//               next id of a global work queue (join order), probes its own
-//               join's table and chains its output offset by look-back only
-//               within its join; the last tile of a join stores its count.
+//   count       one launch over every join's probe tiles: run descriptors and
+//               warp-tile row totals, joins laid out one after the other;
+//   scan        of all the warp-tile totals at once;
+//   write       one launch: a warp tile's offset within its join is the scan
+//               minus the scan at the join's first warp tile; the first warp
+//               tile of a join stores the join's count.
 // Every join's rows are bitwise the same as when it runs alone: the same
 // table order (stable passes over the same rows) and the same tile order.
 #include "ej_device.cuh"
@@ -33,9 +35,10 @@ struct BatchJoin {
   unsigned long long cap;
   unsigned long long* d_count;
   unsigned long long nS;
-  uint32_t first_ptile;  // first probe tile (global work-queue index)
-  uint32_t nptiles;
-  unsigned long long r_row0;  // first row of the join in the concatenated R
+  unsigned long long first_wtile;  // first warp tile of the join in the batch's warp-tile order
+  unsigned long long nwtiles;      // warp tiles of the join
+  unsigned long long desc0;        // first run descriptor of the join in the batch's array
+  unsigned long long r_row0;       // first row of the join in the concatenated R
   const ej_tuple* R;
 };
 
@@ -74,18 +77,40 @@ __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, 
   }
 }
 
-__global__ void __launch_bounds__(PR_THREADS, 3)
-batch_write_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
-                   unsigned long long* lb_status, unsigned int* tile_ctr, ej_dev_status* st) {
-  extern __shared__ __align__(16) unsigned char pw_smem_raw[];
-  PwSmem& sm = *reinterpret_cast<PwSmem*>(pw_smem_raw);
-  if (threadIdx.x == 0) sm.tile = atomicAdd(tile_ctr, 1u);  // global work queue, join by join
-  __syncthreads();
-  const BatchPTile pt = ptiles[sm.tile];
+// count pass over every join's warp tiles (block = one 1024-probe tile of
+// one join), run descriptors into the batch's array
+__global__ void __launch_bounds__(PR_THREADS)
+batch_count_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
+                   unsigned long long* __restrict__ wcount, uint2* __restrict__ desc) {
+  const BatchPTile pt = ptiles[blockIdx.x];
   const BatchJoin& j = joins[pt.join];
-  ej_probe_write_tile<EJ_TABLE_HASH, false>(sm, j.S, (uint64_t)pt.local * PR_TILE, j.nS, j.view,
-                                            lb_status + j.first_ptile, pt.local, pt.local + 1 == j.nptiles, j.out,
-                                            j.cap, j.d_count, st);
+  const uint64_t w = (uint64_t)pt.local * PR_WARPS + (threadIdx.x >> 5);
+  if (w >= j.nwtiles) return;
+  const unsigned long long total =
+      ej_probe_count_warp_desc<EJ_TABLE_HASH, false, true>(j.S, w * PR_WTILE, j.nS, j.view, desc + j.desc0);
+  if ((threadIdx.x & 31u) == 0) wcount[j.first_wtile + w] = total;
+}
+
+// write pass: a warp tile's offset in its join's output is the scan of the
+// batch's warp-tile totals minus the scan at the join's first warp tile
+__global__ void __launch_bounds__(PR_THREADS)
+batch_write_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
+                   const unsigned long long* __restrict__ woff, const uint2* __restrict__ desc, ej_dev_status* st) {
+  __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
+  const BatchPTile pt = ptiles[blockIdx.x];
+  const BatchJoin& j = joins[pt.join];
+  const unsigned int warp = threadIdx.x >> 5;
+  const uint64_t w = (uint64_t)pt.local * PR_WARPS + warp;
+  if (w >= j.nwtiles) return;
+  const unsigned long long base = woff[j.first_wtile];
+  if (w == 0 && (threadIdx.x & 31u) == 0) {
+    const unsigned long long total = woff[j.first_wtile + j.nwtiles] - base;
+    *j.d_count = total;
+    if (total > j.cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  }
+  const unsigned long long off = woff[j.first_wtile + w] - base;
+  if (off >= j.cap) return;
+  ej_probe_write_warp(j.S, desc + j.desc0, w * PR_WTILE, j.nS, j.view, off, j.out, j.cap, stage[warp]);
 }
 
 }  // namespace
@@ -97,7 +122,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   std::vector<ej_rx_tile> rtiles;
   std::vector<BatchPTile> ptiles;
   std::vector<unsigned long long> sbase(n);
-  uint64_t nr_total = 0, start_total = 0, cells = 0;
+  uint64_t nr_total = 0, start_total = 0, cells = 0, nw_total = 0, ns_total = 0;
   for (uint32_t i = 0; i < n; i++) {
     const uint64_t nR = jd[i].nR, nS = jd[i].nS;
     BatchJoin& b = joins[i];
@@ -124,9 +149,13 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     cells += (uint64_t)rt * 256;
     sbase[i] = start_total;
     start_total += (1ull << b.view.hb) + 1;
-    b.first_ptile = (uint32_t)ptiles.size();
-    b.nptiles = (uint32_t)((nS + PR_TILE - 1) / PR_TILE);
-    for (uint32_t t = 0; t < b.nptiles; t++) ptiles.push_back({i, t});
+    b.first_wtile = nw_total;
+    b.nwtiles = (nS + PR_WTILE - 1) / PR_WTILE;
+    nw_total += b.nwtiles;
+    b.desc0 = ns_total;
+    ns_total += nS;
+    const uint32_t nptiles = (uint32_t)((nS + PR_TILE - 1) / PR_TILE);
+    for (uint32_t t = 0; t < nptiles; t++) ptiles.push_back({i, t});
     nr_total += nR;
   }
   if (cells > 0xFFFFFFFFull || nr_total >= 0xFFFFFFFFull)
@@ -150,7 +179,10 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   rp.hist_off = p.add(cells * sizeof(uint32_t));
   rp.offs_off = p.add((cells + 1) * sizeof(uint32_t));
   rp.scan_off = p.add(ej_scan_scratch_bytes(cells));
-  const size_t lb_off = p.add(ptiles.size() * sizeof(unsigned long long) + 16);
+  const size_t wcount_off = p.add((nw_total + 1) * sizeof(unsigned long long));
+  const size_t woff_off = p.add((nw_total + 1) * sizeof(unsigned long long));
+  const size_t wscan_off = p.add(ej_scan_scratch_bytes(nw_total));
+  const size_t desc_off = p.add(std::max<uint64_t>(ns_total, 1) * sizeof(uint2));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
 
   char* A = static_cast<char*>(h->arena);
@@ -203,13 +235,14 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   ej_phase_mark(h, 2);
   ej_phase_mark(h, 3);
   if (!ptiles.empty()) {
-    unsigned long long* lb = reinterpret_cast<unsigned long long*>(A + lb_off);
-    EJ_CUDA(h, cudaMemsetAsync(lb, 0, ptiles.size() * sizeof(unsigned long long) + 16, h->stream));
-    EJ_CUDA(h, cudaFuncSetAttribute(batch_write_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)sizeof(PwSmem)));
-    batch_write_kernel<<<(unsigned)ptiles.size(), PR_THREADS, sizeof(PwSmem), h->stream>>>(
-        djoins, reinterpret_cast<const BatchPTile*>(A + ptiles_off), lb,
-        reinterpret_cast<unsigned int*>(lb + ptiles.size()), h->d_status);
+    unsigned long long* wcount = reinterpret_cast<unsigned long long*>(A + wcount_off);
+    unsigned long long* woff = reinterpret_cast<unsigned long long*>(A + woff_off);
+    uint2* desc = reinterpret_cast<uint2*>(A + desc_off);
+    const BatchPTile* dpt = reinterpret_cast<const BatchPTile*>(A + ptiles_off);
+    batch_count_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, wcount, desc);
+    EJ_TRY(ej_check_launch(h, "batch_count_kernel"));
+    EJ_TRY(ej_scan_u64_u64(h, wcount, nw_total, woff, A + wscan_off));
+    batch_write_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, woff, desc, h->d_status);
     EJ_TRY(ej_check_launch(h, "batch_write_kernel"));
   }
   ej_phase_mark(h, 4);

@@ -1,5 +1,5 @@
-// hash_join.cu - the table build and the probe (count, and write with
-// decoupled look-back) shared by every join that probes R.
+// hash_join.cu - the table build and the probe (count with run descriptors,
+// scan, write) shared by every join that probes R.
 //
 // Reference path replaced (joins/hashJoin_gpu/main_street): radix-partition
 // both relations into ~|R|/64 partitions, split left partitions into 256-tuple
@@ -18,13 +18,15 @@
 //   S      when the table does not fit in L2, S is radix-partitioned once by
 //          the top pb hash bits, so consecutive probe tiles touch one table
 //          region at a time and hit L2; otherwise S is probed in place.
-//   write  one kernel per join: each 1024-probe tile finds its runs, scans
-//          its counts, takes its output offset from the preceding tiles by
-//          decoupled look-back (tiles claim ids in order), then expands the
-//          runs into rows staged in shared memory and written out as
-//          coalesced 16-byte streaming stores (probe_write.cuh).  The
-//          separate count kernel + scan serve the *_count entry points.  Output order is deterministic:
-//          tile, probe, then R run order.
+//   probe  three launches per join (probe_write.cuh): a count pass finds
+//          every probe's run and stores its descriptor (run start, length)
+//          and each 128-probe warp tile's row total; a scan of the totals
+//          gives every warp tile its output offset; the write pass reads the
+//          probes with their descriptors, fetches the run keys and writes the
+//          rows through shared memory as coalesced 16-byte streaming stores.
+//          No warp ever waits for another.  The *_count entry points run the
+//          count pass without descriptors.  Output order is deterministic:
+//          probe order, then R run order.
 // The same kernels serve the sort index (runs by binary search) and the left
 // outer join (OUTER: a probe without matches yields one NULL-extended row).
 #include "ej_device.cuh"
@@ -53,53 +55,43 @@ __global__ void fence_kernel(const int32_t* __restrict__ rval, int32_t* __restri
     fence[i] = rval[(uint64_t)i * EJ_FENCE_STRIDE];
 }
 
-// ---- count (for the *_count entry points) ---------------------------------------
-// Each warp tile's row total; a scan of the totals gives the join's size.
+// ---- count, then write from the run descriptors ---------------------------------
+// (probe_write.cuh); the warp-tile totals are scanned in between
 
-template <int KIND, bool OUTER>
+template <int KIND, bool OUTER, bool DESC>
 __global__ void __launch_bounds__(PR_THREADS)
 probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* __restrict__ wcount,
-                   uint64_t nwtiles) {
+                   uint64_t nwtiles, uint2* __restrict__ desc) {
   const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + (threadIdx.x >> 5);
   if (w >= nwtiles) return;
-  const unsigned long long total = ej_probe_count_warp<KIND, OUTER>(P, w * PR_WTILE, nP, t);
+  const unsigned long long total = ej_probe_count_warp_desc<KIND, OUTER, DESC>(P, w * PR_WTILE, nP, t, desc);
   if ((threadIdx.x & 31u) == 0) wcount[w] = total;
 }
 
-// ---- write with decoupled look-back ---------------------------------------------
-
-template <int KIND, bool OUTER>
-__global__ void __launch_bounds__(PR_THREADS, 3)
-probe_write_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* lb_status,
-                   unsigned int* tile_ctr, uint64_t ntiles, ej_result* __restrict__ out, uint64_t cap,
-                   unsigned long long* d_total, ej_dev_status* st) {
-  extern __shared__ __align__(16) unsigned char pw_smem_raw[];
-  PwSmem& sm = *reinterpret_cast<PwSmem*>(pw_smem_raw);
-  if (threadIdx.x == 0) sm.tile = atomicAdd(tile_ctr, 1u);  // tiles claim ids in launch order (look-back progress)
-  __syncthreads();
-  const uint64_t tile = sm.tile;
-  ej_probe_write_tile<KIND, OUTER>(sm, P, tile * PR_TILE, nP, t, lb_status, tile, tile == ntiles - 1, out, cap,
-                                   d_total, st);
+__global__ void __launch_bounds__(PR_THREADS)
+probe_write_kernel(const ej_tuple* __restrict__ P, const uint2* __restrict__ desc, uint64_t nP, ej_table_view t,
+                   const unsigned long long* __restrict__ woff, uint64_t nwtiles, ej_result* __restrict__ out,
+                   uint64_t cap, ej_dev_status* st) {
+  __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
+  const unsigned int warp = threadIdx.x >> 5;
+  const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + warp;
+  if (w >= nwtiles) return;
+  if (w == 0 && threadIdx.x == 0 && woff[nwtiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  const unsigned long long off = woff[w];
+  if (off >= cap) return;
+  ej_probe_write_warp(P, desc, w * PR_WTILE, nP, t, off, out, cap, stage[warp]);
 }
 
 template <int KIND, bool OUTER>
 ej_status launch_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                       unsigned long long* wcount) {
-  probe_count_kernel<KIND, OUTER><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles);
+                       unsigned long long* wcount, uint2* desc) {
+  if (desc)
+    probe_count_kernel<KIND, OUTER, true>
+        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, desc);
+  else
+    probe_count_kernel<KIND, OUTER, false>
+        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, nullptr);
   return ej_check_launch(h, "probe_count_kernel");
-}
-
-template <int KIND, bool OUTER>
-ej_status launch_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                       ej_result* out, uint64_t cap, unsigned long long* d_total) {
-  unsigned long long* lb = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.lb_off));
-  unsigned int* ctr = reinterpret_cast<unsigned int*>(lb + pp.ntiles);
-  EJ_CUDA(h, cudaMemsetAsync(lb, 0, pp.ntiles * sizeof(unsigned long long) + 16, h->stream));
-  auto k = probe_write_kernel<KIND, OUTER>;
-  EJ_CUDA(h, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PwSmem)));
-  k<<<(unsigned)pp.ntiles, PR_THREADS, sizeof(PwSmem), h->stream>>>(P, pp.nP, t, lb, ctr, pp.ntiles, out, cap,
-                                                                     d_total, h->d_status);
-  return ej_check_launch(h, "probe_write_kernel");
 }
 
 }  // namespace
@@ -190,27 +182,29 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
 
 uint64_t ej_probe_tiles(uint64_t nP) { return (nP + PR_TILE - 1) / PR_TILE; }
 
-void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP) {
+void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP, bool with_desc) {
   pp.nP = nP;
   pp.ntiles = ej_probe_tiles(nP);
   pp.nwtiles = (nP + PR_WTILE - 1) / PR_WTILE;
   pp.count_off = p.add((pp.nwtiles + 1) * sizeof(unsigned long long));
   pp.off_off = p.add((pp.nwtiles + 1) * sizeof(unsigned long long));
   pp.scan_off = p.add(ej_scan_scratch_bytes(pp.nwtiles));
-  pp.lb_off = p.add(pp.ntiles * sizeof(unsigned long long) + 16);
+  pp.with_desc = with_desc;
+  if (with_desc) pp.desc_off = p.add((size_t)(nP ? nP : 1) * sizeof(uint2));
 }
 
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                          bool outer, unsigned long long* d_count) {
   unsigned long long* wcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.count_off));
   unsigned long long* woff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.off_off));
+  uint2* desc = pp.with_desc ? reinterpret_cast<uint2*>(ej_arena_at(h, pp.desc_off)) : nullptr;
   if (pp.ntiles) {
     if (t.kind == EJ_TABLE_HASH)
-      EJ_TRY(outer ? launch_count<EJ_TABLE_HASH, true>(h, pp, P, t, wcount)
-                   : launch_count<EJ_TABLE_HASH, false>(h, pp, P, t, wcount));
+      EJ_TRY(outer ? launch_count<EJ_TABLE_HASH, true>(h, pp, P, t, wcount, desc)
+                   : launch_count<EJ_TABLE_HASH, false>(h, pp, P, t, wcount, desc));
     else
-      EJ_TRY(outer ? launch_count<EJ_TABLE_SORTED, true>(h, pp, P, t, wcount)
-                   : launch_count<EJ_TABLE_SORTED, false>(h, pp, P, t, wcount));
+      EJ_TRY(outer ? launch_count<EJ_TABLE_SORTED, true>(h, pp, P, t, wcount, desc)
+                   : launch_count<EJ_TABLE_SORTED, false>(h, pp, P, t, wcount, desc));
   }
   EJ_TRY(ej_scan_u64_u64(h, wcount, pp.nwtiles, woff, ej_arena_at(h, pp.scan_off)));
   if (d_count)
@@ -220,16 +214,14 @@ ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
 }
 
 ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                         bool outer, ej_result* out, uint64_t cap, unsigned long long* d_count) {
-  if (!pp.ntiles) {
-    EJ_CUDA(h, cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), h->stream));
-    return EJ_OK;
-  }
-  if (t.kind == EJ_TABLE_HASH)
-    return outer ? launch_write<EJ_TABLE_HASH, true>(h, pp, P, t, out, cap, d_count)
-                 : launch_write<EJ_TABLE_HASH, false>(h, pp, P, t, out, cap, d_count);
-  return outer ? launch_write<EJ_TABLE_SORTED, true>(h, pp, P, t, out, cap, d_count)
-               : launch_write<EJ_TABLE_SORTED, false>(h, pp, P, t, out, cap, d_count);
+                         ej_result* out, uint64_t cap) {
+  if (!pp.ntiles) return EJ_OK;
+  if (!pp.with_desc) return ej_fail(h, EJ_ERR_INTERNAL, "probe write planned without run descriptors");
+  const uint2* desc = reinterpret_cast<const uint2*>(ej_arena_at(h, pp.desc_off));
+  const unsigned long long* woff = reinterpret_cast<const unsigned long long*>(ej_arena_at(h, pp.off_off));
+  probe_write_kernel<<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, desc, pp.nP, t, woff, pp.nwtiles, out,
+                                                                        cap, h->d_status);
+  return ej_check_launch(h, "probe_write_kernel");
 }
 
 // ---- partition bits for the probe side ------------------------------------
@@ -252,17 +244,17 @@ uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS) {
 
 // ---- probe drivers -------------------------------------------------------
 
-void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb) {
+void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only) {
   L.pb = pb;
   if (pb) {
     L.spart_off = p.add((size_t)nS * sizeof(ej_tuple));
     ej_radix_plan_add(p, L.splan, nS);
   }
-  ej_probe_plan(p, L.pp, nS);
+  ej_probe_plan(p, L.pp, nS, !count_only);
 }
 
-// Partition S (when the layout says so), then either count (+ scan) or write
-// with look-back; records phase marks 2..4 (the caller has begun the set and
+// Partition S (when the layout says so), count (+ scan), then write unless
+// counting only; records phase marks 2..4 (the caller has begun the set and
 // marked the build).  The arena must already hold the layout, reserved
 // together with anything the table placed there, so that no reservation
 // moves a built table.
@@ -276,13 +268,9 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
     P = spart;
   }
   ej_phase_mark(h, 2);
-  if (count_only) {
-    EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
-    ej_phase_mark(h, 3);
-  } else {
-    ej_phase_mark(h, 3);
-    EJ_TRY(ej_probe_write(h, L.pp, P, t, outer, out, out_cap, d_count));
-  }
+  EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
+  ej_phase_mark(h, 3);
+  if (!count_only) EJ_TRY(ej_probe_write(h, L.pp, P, t, out, out_cap));
   ej_phase_mark(h, 4);
   return EJ_OK;
 }
@@ -295,7 +283,7 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   ej_table_plan_t tp;
   ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR));
   ej_probe_layout L;
-  ej_probe_layout_add(p, L, nS, pb);
+  ej_probe_layout_add(p, L, nS, pb, mode == 2);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t;

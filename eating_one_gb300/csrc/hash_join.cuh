@@ -22,7 +22,9 @@ struct ej_probe_plan_t {
   uint64_t nP = 0;
   uint64_t ntiles = 0;   // blocks of 1024 probes
   uint64_t nwtiles = 0;  // warp tiles of 128 probes
-  size_t count_off = 0, off_off = 0, scan_off = 0, lb_off = 0;
+  size_t count_off = 0, off_off = 0, scan_off = 0;
+  bool with_desc = false;  // run descriptors for the write pass
+  size_t desc_off = 0;
 };
 
 struct ej_probe_layout {
@@ -42,17 +44,18 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
                          void* aux, ej_table_view* view);
 
 uint64_t ej_probe_tiles(uint64_t nP);
-void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP);
-// count pass + scan of the warp-tile totals; the total goes to *d_count (device)
-// when d_count != nullptr
+void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP, bool with_desc);
+// count pass (storing run descriptors when planned with them) + scan of the
+// warp-tile totals; the total goes to *d_count (device) when d_count != nullptr
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                          bool outer, unsigned long long* d_count);
-// write pass with decoupled look-back; the total goes to *d_count (device)
+// write pass from the run descriptors and offsets of ej_probe_count (same
+// plan, same inputs)
 ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                         bool outer, ej_result* out, uint64_t cap, unsigned long long* d_count);
+                         ej_result* out, uint64_t cap);
 
 uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS);
-void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb);
+void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only);
 ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_view& t, const ej_tuple* S,
                         bool outer, bool count_only, ej_result* out, uint64_t out_cap,
                         unsigned long long* d_count);

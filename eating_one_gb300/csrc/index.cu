@@ -100,7 +100,7 @@ static ej_status index_probe(ej_handle* h, const ej_index* ix, const ej_tuple* S
   const uint32_t pb = ix->kind == EJ_TABLE_HASH ? ej_probe_partition_bits(h, ix->nR, nS) : 0u;
   ej_plan_bytes p;
   ej_probe_layout L;
-  ej_probe_layout_add(p, L, nS, pb);
+  ej_probe_layout_add(p, L, nS, pb, count_only);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_phase_mark(h, 1);
@@ -160,7 +160,7 @@ extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_
   ej_table_plan_t tp;
   ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR));
   ej_probe_layout L;
-  ej_probe_layout_add(p, L, nS, pb);
+  ej_probe_layout_add(p, L, nS, pb, /*count_only=*/false);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t;
