@@ -79,7 +79,7 @@ __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, 
 
 // count pass over every join's warp tiles (block = one 1024-probe tile of
 // one join), run descriptors into the batch's array
-__global__ void __launch_bounds__(PR_THREADS)
+__global__ void __launch_bounds__(PR_THREADS, 5)
 batch_count_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
                    unsigned long long* __restrict__ wcount, uint2* __restrict__ desc) {
   const BatchPTile pt = ptiles[blockIdx.x];

@@ -59,7 +59,7 @@ __global__ void fence_kernel(const int32_t* __restrict__ rval, int32_t* __restri
 // (probe_write.cuh); the warp-tile totals are scanned in between
 
 template <int KIND, bool OUTER, bool DESC>
-__global__ void __launch_bounds__(PR_THREADS)
+__global__ void __launch_bounds__(PR_THREADS, 5)  // 40 warps per SM hide the table loads
 probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* __restrict__ wcount,
                    uint64_t nwtiles, uint2* __restrict__ desc) {
   const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + (threadIdx.x >> 5);
