@@ -56,24 +56,24 @@ __global__ void batch_gather_kernel(const ej_rx_tile* __restrict__ tiles, const 
   for (uint32_t i = threadIdx.x; i < d.n; i += blockDim.x) dst[i] = __ldcs(src + i);
 }
 
-// bucket starts of every join: the block of one R tile fills the gaps
+// bucket bounds of every join: the block of one R tile fills the gaps
 // between the buckets of consecutive rows of its join; the join's last row
 // also fills the tail up to 2^hb
 __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, const BatchJoin* __restrict__ joins,
-                                          uint32_t* __restrict__ start_all, const unsigned long long* start_base) {
+                                          uint2* __restrict__ bucket_all, const unsigned long long* bucket_base) {
   const ej_rx_tile d = tiles[blockIdx.x];
   const BatchJoin& j = joins[d.pad];
   const ej_table_view& t = j.view;
-  uint32_t* start = start_all + start_base[d.pad];
+  uint2* bucket = bucket_all + bucket_base[d.pad];
   const uint64_t first = d.start - j.r_row0;  // local row index of the tile's first row
   const int64_t nb = (int64_t)1 << t.hb;
   for (uint32_t i = threadIdx.x; i < d.n; i += blockDim.x) {
     const uint64_t r = first + i;
     const int64_t cur = (int64_t)ej_bucket_of(t.rval[r], t.hb);
     const int64_t prev = r > 0 ? (int64_t)ej_bucket_of(t.rval[r - 1], t.hb) : -1;
-    for (int64_t b = prev + 1; b <= cur; b++) start[b] = (uint32_t)r;
+    for (int64_t b = prev + 1; b <= cur; b++) ej_set_bucket_begin(bucket, b, nb, (uint32_t)r);
     if (r + 1 == t.nR)
-      for (int64_t b = cur + 1; b <= nb; b++) start[b] = (uint32_t)t.nR;
+      for (int64_t b = cur + 1; b <= nb; b++) ej_set_bucket_begin(bucket, b, nb, (uint32_t)t.nR);
   }
 }
 
@@ -148,7 +148,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     }
     cells += (uint64_t)rt * 256;
     sbase[i] = start_total;
-    start_total += (1ull << b.view.hb) + 1;
+    start_total += 1ull << b.view.hb;
     b.first_wtile = nw_total;
     b.nwtiles = (nS + PR_WTILE - 1) / PR_WTILE;
     nw_total += b.nwtiles;
@@ -172,7 +172,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   const size_t tmpb_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
   const size_t rkey_off = p.add(ej_table_col_bytes(nr_total));
   const size_t rval_off = p.add(ej_table_col_bytes(nr_total));
-  const size_t start_off = p.add(start_total * sizeof(uint32_t));
+  const size_t start_off = p.add(start_total * sizeof(uint2));
   ej_radix_plan rp;
   rp.n = nr_total;
   rp.ntiles = (uint32_t)rtiles.size();
@@ -188,13 +188,13 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   char* A = static_cast<char*>(h->arena);
   int32_t* rkey = reinterpret_cast<int32_t*>(A + rkey_off);
   int32_t* rval = reinterpret_cast<int32_t*>(A + rval_off);
-  uint32_t* start = reinterpret_cast<uint32_t*>(A + start_off);
+  uint2* bucket = reinterpret_cast<uint2*>(A + start_off);
   for (uint32_t i = 0; i < n; i++) {
     BatchJoin& b = joins[i];
     b.view.rkey = rkey + b.r_row0;
     b.view.rval = rval + b.r_row0;
     b.view.voff = (uint32_t)(b.r_row0 & 3u);  // the arena column is 16-byte aligned
-    b.view.start = start + sbase[i];
+    b.view.bucket = bucket + sbase[i];
   }
   // descriptors go up with the batch (stream-ordered copies)
   const size_t jb = n * sizeof(BatchJoin), rb = rtiles.size() * sizeof(ej_rx_tile),
@@ -225,10 +225,10 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     }
   }
   // joins with an empty R keep all-zero bucket starts
-  EJ_CUDA(h, cudaMemsetAsync(start, 0, start_total * sizeof(uint32_t), h->stream));
+  EJ_CUDA(h, cudaMemsetAsync(bucket, 0, start_total * sizeof(uint2), h->stream));
   if (!rtiles.empty()) {
     batch_bucket_start_kernel<<<(unsigned)rtiles.size(), 256, 0, h->stream>>>(
-        drt, djoins, start, reinterpret_cast<const unsigned long long*>(A + sbase_off));
+        drt, djoins, bucket, reinterpret_cast<const unsigned long long*>(A + sbase_off));
     EJ_TRY(ej_check_launch(h, "batch_bucket_start_kernel"));
   }
   ej_phase_mark(h, 1);

@@ -142,7 +142,8 @@ ej_status ej_radix_pass_soa(ej_handle* h, const ej_radix_plan& rp, const ej_tupl
 // ---- probe targets (hash_join.cu) -----------------------------------------
 // R is stored as two arrays, rkey[] and rval[], in one order:
 // EJ_TABLE_HASH: sorted by hash32(val), so equal keys form one contiguous run
-//   and bucket b (top `hb` hash bits) is [start[b], start[b+1]).
+//   and bucket b (top `hb` hash bits) is rows [bucket[b].x, bucket[b].y)
+//   (both bounds in one 8-byte word, so a probe reads them with one load).
 // EJ_TABLE_SORTED: sorted by val; the run of a value is found by binary
 //   search, narrowed first by a fence of every 256th val.
 // Both arrays carry EJ_TABLE_PAD readable elements past nR (vector loads).
@@ -153,7 +154,7 @@ struct ej_table_view {
   int kind = EJ_TABLE_HASH;
   const int32_t* rkey = nullptr;     // [nR + pad] row ids in table order
   const int32_t* rval = nullptr;     // [nR + pad] join keys in table order
-  const uint32_t* start = nullptr;   // [2^hb + 1] (hash)
+  const uint2* bucket = nullptr;     // [2^hb] (hash): row bounds of each bucket
   const int32_t* fence = nullptr;    // [nfence] (sorted)
   uint64_t nR = 0;
   uint32_t hb = 1;

@@ -37,15 +37,16 @@
 namespace {
 
 
-// start[b] = first position of bucket b in the hash-sorted table, b in [0, 2^hb].
-__global__ void bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint32_t* __restrict__ start,
+// Row bounds of every bucket of the hash-sorted table: row i (i = nR: the
+// end) begins the buckets between the bucket of row i - 1 and its own.
+__global__ void bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket,
                                     uint32_t hb) {
   const int64_t nbuckets = (int64_t)1 << hb;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nR;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const int64_t cur = i < nR ? (int64_t)ej_bucket_of(rval[i], hb) : nbuckets;
     const int64_t prev = i > 0 ? (int64_t)ej_bucket_of(rval[i - 1], hb) : -1;
-    for (int64_t b = prev + 1; b <= cur; b++) start[b] = (uint32_t)i;
+    for (int64_t b = prev + 1; b <= cur; b++) ej_set_bucket_begin(bucket, b, nbuckets, (uint32_t)i);
   }
 }
 
@@ -107,7 +108,7 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta) {
 // ---- table build --------------------------------------------------------
 
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
-  return tp.kind == EJ_TABLE_HASH ? ((size_t(1) << tp.hb) + 1) * sizeof(uint32_t)
+  return tp.kind == EJ_TABLE_HASH ? (size_t(1) << tp.hb) * sizeof(uint2)
                                   : (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
 }
 
@@ -132,7 +133,7 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
 
 size_t ej_table_bytes(uint64_t nR, int delta) {
   const uint32_t hb = ej_table_bucket_bits(nR, delta);
-  return (size_t)nR * sizeof(ej_tuple) + ((size_t(1) << hb) + 1) * sizeof(uint32_t);
+  return (size_t)nR * sizeof(ej_tuple) + (size_t(1) << hb) * sizeof(uint2);
 }
 
 ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, int32_t* rkey, int32_t* rval,
@@ -159,12 +160,12 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
   view->nR = tp.nR;
   view->hb = tp.hb;
   if (tp.kind == EJ_TABLE_HASH) {
-    uint32_t* start = static_cast<uint32_t*>(aux);
+    uint2* bucket = static_cast<uint2*>(aux);
     const uint64_t work = tp.nR + 1;
     const unsigned blocks = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)h->num_sms * 16);
-    bucket_start_kernel<<<blocks, 256, 0, h->stream>>>(rval, tp.nR, start, tp.hb);
+    bucket_start_kernel<<<blocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb);
     EJ_TRY(ej_check_launch(h, "bucket_start_kernel"));
-    view->start = start;
+    view->bucket = bucket;
   } else {
     int32_t* fence = static_cast<int32_t*>(aux);
     if (tp.nfence) {

@@ -3,8 +3,9 @@
 // A table stores R as rkey[]/rval[] in one order (ej_table_view).  In both
 // kinds the matches of a value v form one contiguous run [lo, lo + c):
 //   EJ_TABLE_HASH    rows sorted by hash32(val); the run lies inside bucket
-//                    b = top hb hash bits, [start[b], start[b+1]), found by
-//                    scanning the bucket with 16-byte vector loads of rval;
+//                    b = top hb hash bits, rows [bucket[b].x, bucket[b].y)
+//                    (one 8-byte load), found by scanning the bucket with
+//                    16-byte vector loads of rval;
 //   EJ_TABLE_SORTED  rows sorted by val; lower and upper bounds by binary
 //                    search, first over the fence (every 256th val), then
 //                    inside one 256-row segment.
@@ -14,6 +15,14 @@
 
 __device__ __forceinline__ uint32_t ej_bucket_of(int32_t val, uint32_t hb) {
   return ej_hash32((uint32_t)val) >> (32u - hb);
+}
+
+// Table build: bucket b begins at row i, so bucket[b].x = i (b < nb) and the
+// previous bucket ends there, bucket[b - 1].y = i (b > 0).
+__device__ __forceinline__ void ej_set_bucket_begin(uint2* bucket, int64_t b, int64_t nb, uint32_t i) {
+  uint32_t* w = reinterpret_cast<uint32_t*>(bucket);
+  if (b < nb) w[2 * b] = i;
+  if (b > 0) w[2 * b - 1] = i;
 }
 
 template <int KIND>
@@ -30,9 +39,9 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
   for (int j = 0; j < N; j++) {
     s0[j] = s1[j] = 0;
     if (ok[j]) {
-      const uint32_t b = ej_bucket_of(v[j], t.hb);
-      s0[j] = __ldg(t.start + b);
-      s1[j] = __ldg(t.start + b + 1);
+      const uint2 bb = __ldg(t.bucket + ej_bucket_of(v[j], t.hb));
+      s0[j] = bb.x;
+      s1[j] = bb.y;
     }
   }
   // vector loads address the aligned base rval - voff; positions are shifted
