@@ -94,11 +94,9 @@ rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __
 }
 
 struct RxScatterSmem {
-  ej_tuple tile[RX_TILE];              // 32 KB
-  uint16_t perm[RX_TILE];              // sorted position -> tile index
-  uint8_t dtile[RX_TILE];              // digit of each tile index
-  uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];  // 8 KB
-  uint32_t digit_start[RX_MAX_DIGITS];
+  ej_tuple sorted[RX_TILE];                // 32 KB: the tile in digit order
+  uint8_t sdig[RX_TILE];                   // digit of each sorted position
+  uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];   // per-warp digit counters, then bases
   uint32_t gbase[RX_MAX_DIGITS];
   uint32_t warp_tmp[RX_WARPS + 1];
 };
@@ -106,7 +104,7 @@ struct RxScatterSmem {
 // SOA: write the key and val of each tuple to two separate arrays (the last
 // pass of a table build) instead of tuples
 template <int KIND, bool SOA>
-__global__ void __launch_bounds__(RX_THREADS)
+__global__ void __launch_bounds__(RX_THREADS, 4)
 rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __restrict__ tiles,
                   ej_tuple* __restrict__ out, int32_t* __restrict__ out_keys, int32_t* __restrict__ out_vals,
                   const uint32_t* __restrict__ offs, uint32_t ntiles, uint32_t shift, uint32_t mask) {
@@ -115,32 +113,47 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile*
   const uint32_t ndig = mask + 1u;
   const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const RxTile tl = rx_tile(tiles, n, ntiles);
-  const uint64_t tbase = tl.start;
   const uint32_t tile_n = tl.n;
-
-  // 1. stage the tile (coalesced 8-byte loads, streaming: read once)
-  const uint2* src = reinterpret_cast<const uint2*>(in + tbase);
-  uint2* dst = reinterpret_cast<uint2*>(sm.tile);
-#pragma unroll 8
-  for (uint32_t i = threadIdx.x; i < tile_n; i += RX_THREADS) dst[i] = __ldcs(src + i);
   for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&sm.cnt[0][0])[i] = 0u;
-  __syncthreads();
 
-  // 2. digits of the tile (kept in shared memory) and per-warp digit counts
-  //    over the warp's consecutive span; counting order does not matter
+  // 1. the warp's RX_ROUNDS x 32 consecutive tuples into registers (coalesced,
+  //    streaming: read once)
   const uint32_t wbase = warp * RX_WARP_SPAN;
-#pragma unroll 4
+  const uint2* src = reinterpret_cast<const uint2*>(in + tl.start);
+  uint2 tup[RX_ROUNDS];
+#pragma unroll
   for (int r = 0; r < RX_ROUNDS; r++) {
     const uint32_t i = wbase + r * 32u + lane;
-    if (i < tile_n) {
-      const uint32_t d = rx_digit<KIND>(sm.tile[i].val, shift, mask);
-      sm.dtile[i] = (uint8_t)d;
-      atomicAdd(&sm.cnt[warp][d], 1u);
+    tup[r] = i < tile_n ? __ldcs(src + i) : make_uint2(0u, 0u);
+  }
+  __syncthreads();  // counters zeroed
+
+  // 2. stable rank within the warp: round order, then lane order; the lanes
+  //    sharing a digit come from one ballot per digit bit, the warp's running
+  //    count of each digit from its shared-memory counter.  Each item keeps
+  //    (digit << 16 | rank within the warp's items of that digit).
+  uint32_t packed[RX_ROUNDS];
+#pragma unroll
+  for (int r = 0; r < RX_ROUNDS; r++) {
+    const uint32_t i = wbase + r * 32u + lane;
+    const bool valid = i < tile_n;
+    const uint32_t d = valid ? rx_digit<KIND>((int32_t)tup[r].y, shift, mask) : 0u;
+    const unsigned int peers = ej_match_digit<8>(d, __ballot_sync(EJ_FULL_MASK, valid));
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (valid && (int)lane == leader) {
+      old = sm.cnt[warp][d];
+      sm.cnt[warp][d] = old + __popc(peers);
     }
+    old = __shfl_sync(EJ_FULL_MASK, old, leader < 0 ? 0 : leader);
+    packed[r] = valid ? (d << 16) | (old + __popc(peers & ej_lanemask_lt())) : 0xFFFFFFFFu;
+    __syncwarp();
   }
   __syncthreads();
 
-  // 3. warp offsets within each digit, digit starts within the tile, global bases
+  // 3. per digit: warp bases within the digit, the digit's start in the tile
+  //    (cnt[w][d] becomes the tile position of warp w's first item of digit
+  //    d) and the global base of the digit's run
   uint32_t total = 0;
   if (threadIdx.x < ndig) {
     const uint32_t d = threadIdx.x;
@@ -154,40 +167,34 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile*
   uint32_t all;
   const uint32_t dstart = ej_block_exclusive_sum<RX_THREADS, uint32_t>(total, sm.warp_tmp, &all);
   if (threadIdx.x < ndig) {
-    sm.digit_start[threadIdx.x] = dstart;
-    sm.gbase[threadIdx.x] = offs[tl.cell0 + (uint64_t)threadIdx.x * tl.stride] - dstart;
+    const uint32_t d = threadIdx.x;
+#pragma unroll
+    for (int w = 0; w < RX_WARPS; w++) sm.cnt[w][d] += dstart;
+    sm.gbase[d] = offs[tl.cell0 + (uint64_t)d * tl.stride] - dstart;
   }
   __syncthreads();
 
-  // 4. stable rank: warp order, then round order, then lane order; the lanes
-  //    sharing a digit are found with one ballot per digit bit
+  // 4. every item to its sorted position in shared memory
+#pragma unroll
   for (int r = 0; r < RX_ROUNDS; r++) {
-    const uint32_t i = wbase + r * 32u + lane;
-    const bool valid = i < tile_n;
-    const uint32_t d = valid ? sm.dtile[i] : 0u;
-    const unsigned int peers = ej_match_digit<8>(d, __ballot_sync(EJ_FULL_MASK, valid));
-    const int leader = __ffs(peers) - 1;
-    uint32_t old = 0;
-    if (valid && (int)lane == leader) {
-      old = sm.cnt[warp][d];
-      sm.cnt[warp][d] = old + __popc(peers);
+    if (packed[r] != 0xFFFFFFFFu) {
+      const uint32_t d = packed[r] >> 16;
+      const uint32_t pos = sm.cnt[warp][d] + (packed[r] & 0xFFFFu);
+      reinterpret_cast<uint2*>(sm.sorted)[pos] = tup[r];
+      sm.sdig[pos] = (uint8_t)d;
     }
-    old = __shfl_sync(EJ_FULL_MASK, old, leader < 0 ? 0 : leader);
-    if (valid) sm.perm[sm.digit_start[d] + old + __popc(peers & ej_lanemask_lt())] = (uint16_t)i;
-    __syncwarp();
   }
   __syncthreads();
 
   // 5. write digit runs: sorted position k goes to gbase[digit] + k
   for (uint32_t k = threadIdx.x; k < tile_n; k += RX_THREADS) {
-    const uint32_t i = sm.perm[k];
-    const ej_tuple t = sm.tile[i];
-    const uint32_t pos = sm.gbase[sm.dtile[i]] + k;
+    const uint2 t = reinterpret_cast<const uint2*>(sm.sorted)[k];
+    const uint32_t pos = sm.gbase[sm.sdig[k]] + k;
     if (SOA) {
-      out_keys[pos] = t.key;
-      out_vals[pos] = t.val;
+      out_keys[pos] = (int32_t)t.x;
+      out_vals[pos] = (int32_t)t.y;
     } else {
-      reinterpret_cast<uint2*>(out)[pos] = make_uint2((uint32_t)t.key, (uint32_t)t.val);
+      reinterpret_cast<uint2*>(out)[pos] = t;
     }
   }
 }
