@@ -26,6 +26,7 @@
 namespace {
 
 constexpr uint32_t BX_RX_TILE = EJ_RX_TILE;
+static_assert(BX_RX_TILE % 256 == 0, "bucket bounds take 256-row warp spans that must not cross an R tile");
 
 // per join, on the device
 struct BatchJoin {
@@ -66,15 +67,12 @@ __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, 
   const ej_table_view& t = j.view;
   uint2* bucket = bucket_all + bucket_base[d.pad];
   const uint64_t first = d.start - j.r_row0;  // local row index of the tile's first row
-  const int64_t nb = (int64_t)1 << t.hb;
-  for (uint32_t i = threadIdx.x; i < d.n; i += blockDim.x) {
-    const uint64_t r = first + i;
-    const int64_t cur = (int64_t)ej_bucket_of(t.rval[r], t.hb);
-    const int64_t prev = r > 0 ? (int64_t)ej_bucket_of(t.rval[r - 1], t.hb) : -1;
-    for (int64_t b = prev + 1; b <= cur; b++) ej_set_bucket_begin(bucket, b, nb, (uint32_t)r);
-    if (r + 1 == t.nR)
-      for (int64_t b = cur + 1; b <= nb; b++) ej_set_bucket_begin(bucket, b, nb, (uint32_t)t.nR);
-  }
+  // the join's last tile also takes the end row (local row nR)
+  const uint64_t end = first + d.n + (first + d.n == t.nR ? 1u : 0u);
+  // tiles are multiples of 256 rows except a join's last, so a warp's 256
+  // rows never reach into the next tile
+  for (uint64_t r0 = first + (threadIdx.x >> 5) * 256; r0 < end; r0 += (blockDim.x >> 5) * 256)
+    ej_bucket_bounds_warp(t.rval, t.nR, r0, t.hb, bucket);
 }
 
 // count pass over every join's warp tiles (block = one 1024-probe tile of

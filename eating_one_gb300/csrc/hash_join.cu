@@ -38,16 +38,12 @@ namespace {
 
 
 // Row bounds of every bucket of the hash-sorted table: row i (i = nR: the
-// end) begins the buckets between the bucket of row i - 1 and its own.
-__global__ void bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket,
-                                    uint32_t hb) {
-  const int64_t nbuckets = (int64_t)1 << hb;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nR;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const int64_t cur = i < nR ? (int64_t)ej_bucket_of(rval[i], hb) : nbuckets;
-    const int64_t prev = i > 0 ? (int64_t)ej_bucket_of(rval[i - 1], hb) : -1;
-    for (int64_t b = prev + 1; b <= cur; b++) ej_set_bucket_begin(bucket, b, nbuckets, (uint32_t)i);
-  }
+// end) begins the buckets between the bucket of row i - 1 and its own; each
+// warp takes 256 consecutive rows.
+__global__ void __launch_bounds__(256)
+bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb) {
+  const uint64_t r0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * 256;
+  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket);
 }
 
 // fence[i] = rval[i * EJ_FENCE_STRIDE] of a val-sorted table
@@ -161,9 +157,8 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
   view->hb = tp.hb;
   if (tp.kind == EJ_TABLE_HASH) {
     uint2* bucket = static_cast<uint2*>(aux);
-    const uint64_t work = tp.nR + 1;
-    const unsigned blocks = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)h->num_sms * 16);
-    bucket_start_kernel<<<blocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb);
+    const uint64_t blocks = (tp.nR + 1 + 2047) / 2048;  // 256 rows per warp, 8 warps per block
+    bucket_start_kernel<<<(unsigned)blocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb);
     EJ_TRY(ej_check_launch(h, "bucket_start_kernel"));
     view->bucket = bucket;
   } else {

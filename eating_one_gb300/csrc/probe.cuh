@@ -25,6 +25,43 @@ __device__ __forceinline__ void ej_set_bucket_begin(uint2* bucket, int64_t b, in
   if (b > 0) w[2 * b - 1] = i;
 }
 
+// Table build, one warp: the bounds of the buckets that begin at rows
+// [r0, r0 + 256) of a hash-sorted column of n rows; row n (when in range) is
+// the end, which begins the buckets past the last row's.  Lane l looks at
+// rows r0 + 32k + l (coalesced loads, all issued together) and takes the
+// bucket of the row before from its neighbour lane.
+__device__ __forceinline__ void ej_bucket_bounds_warp(const int32_t* __restrict__ rval, uint64_t n, uint64_t r0,
+                                                      uint32_t hb, uint2* __restrict__ bucket) {
+  const unsigned int lane = threadIdx.x & 31u;
+  const int32_t nb = (int32_t)(1u << hb);
+  int32_t cur[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const uint64_t i = r0 + (uint64_t)k * 32 + lane;
+    cur[k] = i < n ? (int32_t)ej_bucket_of(rval[i], hb) : nb;
+  }
+  int32_t carry = -1;  // bucket of row r0 + 32k - 1
+  if (r0 > 0) carry = r0 - 1 < n ? (int32_t)ej_bucket_of(rval[r0 - 1], hb) : nb;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int32_t up = __shfl_up_sync(EJ_FULL_MASK, cur[k], 1);
+    const int32_t prev = lane == 0 ? carry : up;
+    carry = __shfl_sync(EJ_FULL_MASK, cur[k], 31);
+    const uint64_t i = r0 + (uint64_t)k * 32 + lane;
+    // a long run of empty buckets (a heavily duplicated key) is filled by the
+    // whole warp, the rest by each lane
+    const bool wide = i <= n && cur[k] - prev > 32;
+    if (i <= n && !wide)
+      for (int32_t b = prev + 1; b <= cur[k]; b++) ej_set_bucket_begin(bucket, b, nb, (uint32_t)i);
+    for (unsigned int m = __ballot_sync(EJ_FULL_MASK, wide); m; m &= m - 1u) {
+      const int src = __ffs(m) - 1;
+      const int32_t p = __shfl_sync(EJ_FULL_MASK, prev, src), c = __shfl_sync(EJ_FULL_MASK, cur[k], src);
+      const uint32_t row = (uint32_t)__shfl_sync(EJ_FULL_MASK, (unsigned long long)i, src);
+      for (int32_t b = p + 1 + (int32_t)lane; b <= c; b += 32) ej_set_bucket_begin(bucket, b, nb, row);
+    }
+  }
+}
+
 template <int KIND>
 struct EjRun;
 

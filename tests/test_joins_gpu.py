@@ -56,6 +56,7 @@ CASES = [  # (nR, nS, key range) - unique-ish, many-to-many, heavy duplicates, r
     (12345, 54321, (-1000, 1000)),
     (1, 1, (7, 8)),
     (2000, 3000, (0, 8)),  # ~250 rows per probe: groups larger than the write buffer
+    (131072, 20, (5, 8)),  # three keys: long runs of empty buckets in the hash table
 ]
 
 
