@@ -4,14 +4,16 @@
 // run one join, print the phase timers, the result count and the first three
 // result rows (hj.cc:1194-1249).
 //
-//   ej_join <algo> <left> <right> [--seed N] [--domain D] [--host] [--table R.tbl S.tbl]
+//   ej_join <algo> <left> <right> [--seed N] [--domain D] [--host] [--table R.tbl S.tbl] [--raw R S]
 //
 // algo: hash | single_hash | bnl | hash_index | sort_index | left_outer.
 // left = |S| (probe side), right = |R| (build side), as in the reference.
 // Default inputs: R keys a permutation of [0, right), S keys uniform over
 // [0, domain) with domain = right (every S row matches exactly once).
 // --table reads both relations in the reference's table format (int32 count,
-// then TUPLE[count]; joins/hashJoin_gpu/main_street/TableBuild.cpp:118-140).
+// then TUPLE[count]; joins/hashJoin_gpu/main_street/TableBuild.cpp:118-140),
+// --raw as bare TUPLE arrays (the joins/join_ori R and S files); <left> and
+// <right> are then ignored.
 // --host joins host buffers through ej_join_host (copies inside the timing).
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -29,30 +31,22 @@ static void die(ej_handle* h, ej_status s, const char* what) {
   exit(1);
 }
 
-static std::vector<ej_tuple> read_table(const char* path) {
-  FILE* f = fopen(path, "rb");
-  if (!f) {
-    perror(path);
+static std::vector<ej_tuple> read_table(const char* path, ej_table_file_format fmt) {
+  uint64_t n = 0;
+  ej_status st = ej_table_file_rows(path, fmt, &n);
+  std::vector<ej_tuple> t(st == EJ_OK ? (size_t)n : 0);
+  if (st == EJ_OK) st = ej_table_file_read(path, fmt, t.data(), n, &n);
+  if (st != EJ_OK) {
+    fprintf(stderr, "%s: %s\n", path, ej_status_name(st));
     exit(1);
   }
-  int32_t n = 0;
-  if (fread(&n, sizeof n, 1, f) != 1 || n < 0) {
-    fprintf(stderr, "%s: bad table header\n", path);
-    exit(1);
-  }
-  std::vector<ej_tuple> t((size_t)n);
-  if (n && fread(t.data(), sizeof(ej_tuple), (size_t)n, f) != (size_t)n) {
-    fprintf(stderr, "%s: short table\n", path);
-    exit(1);
-  }
-  fclose(f);
   return t;
 }
 
 int main(int argc, char** argv) {
   if (argc < 4) {
     fprintf(stderr, "usage: %s <hash|single_hash|bnl|hash_index|sort_index|left_outer> <left> <right> "
-                    "[--seed N] [--domain D] [--host] [--table R.tbl S.tbl]\n", argv[0]);
+                    "[--seed N] [--domain D] [--host] [--table R.tbl S.tbl] [--raw R S]\n", argv[0]);
     return 2;
   }
   const std::string algo_name = argv[1];
@@ -70,11 +64,13 @@ int main(int argc, char** argv) {
   bool host = false;
   const char* rtab = nullptr;
   const char* stab = nullptr;
+  ej_table_file_format tfmt = EJ_TABLE_FILE_COUNTED;
   for (int i = 4; i < argc; i++) {
     if (!strcmp(argv[i], "--seed") && i + 1 < argc) seed = strtoull(argv[++i], nullptr, 10);
     else if (!strcmp(argv[i], "--domain") && i + 1 < argc) domain = (uint32_t)strtoul(argv[++i], nullptr, 10);
     else if (!strcmp(argv[i], "--host")) host = true;
-    else if (!strcmp(argv[i], "--table") && i + 2 < argc) {
+    else if ((!strcmp(argv[i], "--table") || !strcmp(argv[i], "--raw")) && i + 2 < argc) {
+      tfmt = !strcmp(argv[i], "--raw") ? EJ_TABLE_FILE_RAW : EJ_TABLE_FILE_COUNTED;
       rtab = argv[++i];
       stab = argv[++i];
     }
@@ -89,8 +85,8 @@ int main(int argc, char** argv) {
   std::vector<ej_tuple> hR, hS;
   ej_tuple *R = nullptr, *S = nullptr;
   if (rtab) {
-    hR = read_table(rtab);
-    hS = read_table(stab);
+    hR = read_table(rtab, tfmt);
+    hS = read_table(stab, tfmt);
     right = hR.size();
     left = hS.size();
   }

@@ -44,6 +44,7 @@ extern "C" const char* ej_status_name(ej_status s) {
     case EJ_ERR_NO_DEVICE: return "EJ_ERR_NO_DEVICE";
     case EJ_ERR_BUSY: return "EJ_ERR_BUSY";
     case EJ_ERR_INTERNAL: return "EJ_ERR_INTERNAL";
+    case EJ_ERR_IO: return "EJ_ERR_IO";
   }
   return "EJ_ERR_UNKNOWN";
 }

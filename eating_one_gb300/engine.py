@@ -8,6 +8,7 @@ there is no other implementation of any join.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import torch
 
@@ -224,6 +225,23 @@ class Engine:
         out = torch.empty((spec.n, 2), dtype=torch.int32, device=self.device)
         self._check(self.lib.ej_generate(self.h, C.byref(spec), _ptr(out)))
         return out
+
+    def load_table(self, path: str, fmt: int = native.EJ_TABLE_FILE_COUNTED) -> torch.Tensor:
+        """A table file (include/ej.h: EJ_TABLE_FILE_COUNTED or _RAW) as an (n, 2) int32 device tensor."""
+        self._sync_stream()
+        n = C.c_uint64(0)
+        st = self.lib.ej_table_file_rows(os.fsencode(path), fmt, C.byref(n))
+        if st != native.EJ_OK:
+            raise JoinError(st, "cannot read %s as a table file" % path)
+        out = torch.empty((max(n.value, 1), 2), dtype=torch.int32, device=self.device)[:n.value]
+        self._check(self.lib.ej_table_load(self.h, os.fsencode(path), fmt, _ptr(out), n.value, C.byref(n)))
+        return out
+
+    def save_table(self, path: str, rows: torch.Tensor, fmt: int = native.EJ_TABLE_FILE_COUNTED) -> None:
+        """Write an (n, 2) int32 relation (device or host) as a table file."""
+        self._sync_stream()
+        rows = rows.contiguous()
+        self._check(self.lib.ej_table_save(self.h, os.fsencode(path), fmt, _ptr(rows), rows.shape[0]))
 
     def checksum(self, rows: torch.Tensor) -> int:
         """Order-independent checksum of result rows (same function as the oracle's)."""

@@ -20,6 +20,7 @@ EJ_ERR_TOO_LARGE = 6
 EJ_ERR_NO_DEVICE = 7
 EJ_ERR_BUSY = 8
 EJ_ERR_INTERNAL = 9
+EJ_ERR_IO = 10
 
 ALGO = {"hash": 0, "single_hash": 1, "bnl": 2, "hash_index": 3, "sort_index": 4, "left_outer": 5}
 
@@ -75,6 +76,7 @@ class TuneEntry(C.Structure):
 
 
 EJ_SERVE_BATCHED, EJ_SERVE_PER_JOIN = 0, 1
+EJ_TABLE_FILE_COUNTED, EJ_TABLE_FILE_RAW = 0, 1
 
 _vp, _u64, _pu64, _i32 = C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_int
 
@@ -124,6 +126,10 @@ _SIGS = {
     "ej_exclusive_scan_u32_noalloc": [_vp, _u64, _vp, _vp],
     "ej_generate": [_vp, C.POINTER(GenSpec), _vp],
     "ej_checksum": [_vp, _vp, _u64, C.c_uint32, _pu64],
+    "ej_table_file_rows": [C.c_char_p, _i32, _pu64],
+    "ej_table_file_read": [C.c_char_p, _i32, _vp, _u64, _pu64],
+    "ej_table_load": [_vp, C.c_char_p, _i32, _vp, _u64, _pu64],
+    "ej_table_save": [_vp, C.c_char_p, _i32, _vp, _u64],
 }
 _RESTYPES = {"ej_status_name": C.c_char_p, "ej_last_error": C.c_char_p, "ej_scratch_bytes": C.c_uint64,
              "ej_kernel_launches": C.c_uint64, "ej_now_ns": C.c_uint64}
@@ -153,3 +159,20 @@ def load(path: str | None = None) -> C.CDLL:
     if path is None:
         _lib = lib
     return lib
+
+
+def read_table_file(path: str, fmt: int = EJ_TABLE_FILE_COUNTED):
+    """A table file read into host memory by the library (no GPU needed):
+    an (n, 2) int32 numpy array of TUPLE{key, val} rows."""
+    import numpy as np
+
+    lib = load()
+    n = C.c_uint64(0)
+    st = lib.ej_table_file_rows(os.fsencode(path), fmt, C.byref(n))
+    if st != EJ_OK:
+        raise OSError("%s: %s" % (path, lib.ej_status_name(st).decode()))
+    out = np.empty((n.value, 2), dtype=np.int32)
+    st = lib.ej_table_file_read(os.fsencode(path), fmt, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n))
+    if st != EJ_OK:
+        raise OSError("%s: %s" % (path, lib.ej_status_name(st).decode()))
+    return out

@@ -61,7 +61,8 @@ typedef enum ej_status {
   EJ_ERR_TOO_LARGE = 6, /* input beyond a documented size limit */
   EJ_ERR_NO_DEVICE = 7, /* no CUDA device or not an sm_103 device */
   EJ_ERR_BUSY = 8,      /* serving queue full or admission refused */
-  EJ_ERR_INTERNAL = 9   /* device-side consistency check failed */
+  EJ_ERR_INTERNAL = 9,  /* device-side consistency check failed */
+  EJ_ERR_IO = 10        /* a table file could not be opened, read or written */
 } ej_status;
 
 typedef struct ej_handle ej_handle;
@@ -322,6 +323,30 @@ ej_status ej_generate(ej_handle* h, const ej_gen_spec* spec, ej_tuple* out);
  * function as the oracle's), for comparing result multisets without sorting. */
 ej_status ej_checksum(ej_handle* h, const void* rows, uint64_t nrows, uint32_t words_per_row,
                       uint64_t* out_sum);
+
+/* ---- on-disk relations ----------------------------------------------------
+ * The reference's two table formats (little-endian):
+ *   EJ_TABLE_FILE_COUNTED  int32 n, then n tuples: written by
+ *                          joins/hashJoin_gpu/main_street/TableBuild.cpp:113-140,
+ *                          read by joins/hashJoin_gpu/disk_hash/hj.cc:212-266;
+ *   EJ_TABLE_FILE_RAW      tuples only, n = file size / 8: joins/join_ori/R and S,
+ *                          read by joins/join_ori/hj.cc:68-78.
+ * The reference reads these with fread/read inside each executable; these entry
+ * points replace those loops.  A missing, truncated or malformed file returns
+ * EJ_ERR_IO; more rows than cap return EJ_ERR_CAPACITY with *n set. */
+typedef enum { EJ_TABLE_FILE_COUNTED = 0, EJ_TABLE_FILE_RAW = 1 } ej_table_file_format;
+/* Rows of a table file (host only, no handle). */
+ej_status ej_table_file_rows(const char* path, ej_table_file_format fmt, uint64_t* n);
+/* Read a table file into host memory (host only, no handle). */
+ej_status ej_table_file_read(const char* path, ej_table_file_format fmt, ej_tuple* dst, uint64_t cap, uint64_t* n);
+/* Load a table file into device memory: the file streams through two pinned
+ * 32 MiB buffers, each read overlapping the copy of the previous chunk on the
+ * handle's stream; returns when dst holds the rows. */
+ej_status ej_table_load(ej_handle* h, const char* path, ej_table_file_format fmt, ej_tuple* dst, uint64_t cap,
+                        uint64_t* n);
+/* Write n rows (device or host memory) as a table file; from device memory
+ * each chunk's copy overlaps the write of the previous one. */
+ej_status ej_table_save(ej_handle* h, const char* path, ej_table_file_format fmt, const ej_tuple* src, uint64_t n);
 
 #ifdef __cplusplus
 }
