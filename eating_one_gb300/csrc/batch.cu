@@ -230,8 +230,8 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     EJ_TRY(ej_check_launch(h, "batch_bucket_start_kernel"));
   }
   ej_phase_mark(h, 1);
-  ej_phase_mark(h, 2);
-  ej_phase_mark(h, 3);
+  ej_phase_mark(h, 2);  // no partition pass: every table of a batch is probed in place
+  if (ptiles.empty()) ej_phase_mark(h, 3);
   if (!ptiles.empty()) {
     unsigned long long* wcount = reinterpret_cast<unsigned long long*>(A + wcount_off);
     unsigned long long* woff = reinterpret_cast<unsigned long long*>(A + woff_off);
@@ -240,6 +240,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     batch_count_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, wcount, desc);
     EJ_TRY(ej_check_launch(h, "batch_count_kernel"));
     EJ_TRY(ej_scan_u64_u64(h, wcount, nw_total, woff, A + wscan_off));
+    ej_phase_mark(h, 3);
     batch_write_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, woff, desc, h->d_status);
     EJ_TRY(ej_check_launch(h, "batch_write_kernel"));
   }
