@@ -139,64 +139,98 @@ def gather_ms(ms: float, dist, device) -> list[float]:
     return [float(x.item()) for x in g]
 
 
-def cpu_baseline_sample(scale: int = 4) -> dict:
-    """The oracle's hash_cpu restatement on a 1/2^scale-size sample of every
-    variant (generation excluded, as the reference times it), one thread each."""
-    import numpy as np  # noqa: F401
+def _cpu_join_timed(R, S, threads: int) -> tuple[float, int]:
+    """One oracle join into a preallocated, already-touched output (the
+    reference materialises into a calloc'd result array too); returns
+    (seconds, rows).  threads 0: the single-threaded joins/CPU_JOIN/hash_cpu
+    restatement; else the pthread joins/multi_joins/hash restatement."""
+    import ctypes as C
 
+    import numpy as np
+
+    from oracle import oracle as O
+
+    lib = O.load()
+    R = np.ascontiguousarray(R, dtype=np.int32)
+    S = np.ascontiguousarray(S, dtype=np.int32)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+
+    def call(out, cap):
+        if threads:
+            return lib.ejo_hash_join_mt(p(R), len(R), p(S), len(S), out, cap, 1 << 17, threads)
+        return lib.ejo_hash_join(p(R), len(R), p(S), len(S), out, cap, 1 << 20)
+
+    n = int(call(None, 0))
+    out = np.ones((max(n, 1), 4), dtype=np.int32)  # touched before the clock starts
+    t0 = time.perf_counter()
+    m = int(call(p(out), n))
+    dt = time.perf_counter() - t0
+    assert m == n
+    return dt, n
+
+
+def _cpu_rels(scale: int):
     from eating_one_gb300.workloads import workload
     from oracle import oracle as O
 
-    rels = []
-    for v in VARIANTS:
-        w = workload(v, scale)
-        rels.append((O.generate(w["R"]), O.generate(w["S"])))
+    return [(O.generate(workload(v, scale)["R"]), O.generate(workload(v, scale)["S"])) for v in VARIANTS]
+
+
+def cpu_baseline_sample(scale: int = 4, rels=None) -> dict:
+    """The oracle's hash_cpu restatement on a 1/2^scale-size sample of every
+    variant (generation excluded, as the reference times it), one thread each."""
+    rels = rels or _cpu_rels(scale)
     results = [None] * len(rels)
 
     def one(i):
         R, S = rels[i]
-        t0 = time.perf_counter()
-        rows = O.hash_join(R, S)
-        results[i] = (time.perf_counter() - t0, len(R) + len(S), len(rows))
+        dt, n = _cpu_join_timed(R, S, 0)
+        results[i] = (dt, len(R) + len(S), n)
 
     threads = [threading.Thread(target=one, args=(i,)) for i in range(len(rels))]
-    t0 = time.perf_counter()
     for t in threads:
         t.start()
     for t in threads:
         t.join()
-    wall = time.perf_counter() - t0
+    wall = max(r[0] for r in results)
     tuples = sum(r[1] for r in results)
     return {"value": tuples / wall, "unit": UNIT, "cores": len(rels), "kind": "port",
             "sample": "oracle restatement of joins/CPU_JOIN/hash_cpu (partition by val %% 2^20 + bucket "
-                      "nested loop, rows materialised) on the three C3 variants at 1/%d size (R=2^%d, "
-                      "S=2^%d), one host thread per variant, generation excluded" % (2 ** scale, 26 - scale,
-                                                                                  28 - scale),
+                      "nested loop, rows materialised into a preallocated array) on the three C3 variants at "
+                      "1/%d size (R=2^%d, S=2^%d), one host thread per variant, generation excluded"
+                      % (2 ** scale, 26 - scale, 28 - scale),
             "seconds": round(wall, 3), "rows": sum(r[2] for r in results)}
 
 
 def run_reference(args) -> None:
-    """Reference arm: the reference CPU hash join (restated; the reference's own
-    binaries cannot be built where /root/reference is absent) on bounded samples."""
+    """Reference arm: the reference's multithreaded CPU hash join
+    (joins/multi_joins/hash, restated; the reference's own binaries cannot be
+    built where the reference sources are absent) with every host core, on a
+    bounded 1/16-size sample of the three C3 variants per step."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
-    scale = 6
+    scale = 4
+    nt = os.cpu_count() or 8
+    rels = _cpu_rels(scale)
+
+    def step():
+        return sum(_cpu_join_timed(R, S, nt)[0] for R, S in rels)
+
     for _ in range(args.warmup):
-        cpu_baseline_sample(scale)
-    vals, secs = [], []
-    for _ in range(args.steps):
-        r = cpu_baseline_sample(scale)
-        vals.append(r["value"])
-        secs.append(r["seconds"])
-    total_tuples = 3 * ((1 << (26 - scale)) + (1 << (28 - scale)))
+        step()
+    secs = [step() for _ in range(args.steps)]
+    total_tuples = sum(len(R) + len(S) for R, S in rels)
     value = total_tuples * len(secs) / sum(secs)
+    sample = ("oracle restatement of joins/multi_joins/hash (pthreads: partition by val %% 2^17 with per-thread "
+              "counts and scatter, partitions claimed by threads and nested-looped, rows materialised into a "
+              "preallocated array) on the three C3 variants at 1/%d size (R=2^%d, S=2^%d), %d threads, "
+              "generation excluded" % (2 ** scale, 26 - scale, 28 - scale, nt))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(secs) / len(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic", "config": {"workload": WORKLOAD + " (CPU sample at 1/64 size)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 3, "kind": "port",
-                             "sample": r["sample"].replace("1/16", "1/64")},
+            "data": "synthetic", "config": {"workload": WORKLOAD + " (CPU sample at 1/%d size)" % 2 ** scale},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

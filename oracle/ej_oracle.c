@@ -29,12 +29,20 @@
  *     bidx+1 == right (joins/CPU_JOIN/sortIndex_cpu/inner-idx-bnlj.cc:226-227);
  *     the restatement checks the bound first.
  *   - counts and offsets are 64-bit (the reference uses int/uint).
+ *   - the multithreaded hash join counts each partition's matches, then
+ *     writes them at the partition's offset (rows in partition order); the
+ *     reference appends every row to one array under one mutex
+ *     (joins/multi_joins/hash/thread-hash-bnlj.cc:334-349), which only
+ *     serialises it and makes the row order depend on thread timing.  Its lpartitioning
+ *     clamps the probe side's chunk end to the build side's size (:190-200);
+ *     the restatement clamps to the probe side's.
  *   - the left outer join and the 3-way star join have no reference
  *     implementation (joins/outerJoin_gpu computes an inner join); their
  *     semantics here are defined by this file: outer = inner join plus
  *     (INT32_MIN, INT32_MIN, s.key, s.val) for every unmatched S row;
  *     star = both dimension probes of each fact row, cross product of matches.
  */
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -105,6 +113,148 @@ uint64_t ejo_hash_join(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint
 done:
   free(hrt); free(hlt); free(rloc); free(rcnt); free(lloc); free(lcnt);
   return n;
+}
+
+/* ---------------------------------------------------------------------------
+ * Multithreaded partitioned hash join: joins/multi_joins/hash/thread-hash-bnlj.cc
+ *   l/rcount_partitioning (:146-179, :219-252): thread t counts val % PARTITION
+ *   over its contiguous chunk into L[p * THREAD_NUM + t]; createThreads
+ *   (:393-396, :440-443): exclusive prefix of those counts; l/rpartitioning
+ *   (:181-217, :254-290): thread t scatters its chunk at the running offsets;
+ *   RTGetter + executor (:292-362): threads take partitions one at a time from
+ *   a shared counter and nested-loop each partition's S rows against its R
+ *   rows.  partitions = PARTITION (2^17), threads = THREAD_NUM (8 there).
+ * Returns the number of matches; writes min(matches, cap) rows in partition
+ * order (out NULL or cap 0: counts only).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  const ejo_tuple* in;
+  uint64_t n, lo, hi;   /* this thread's chunk of in */
+  uint32_t np, t, nt;
+  uint64_t* cnt;        /* [np * nt], partition-major */
+  ejo_tuple* out;
+} mt_part_arg;
+
+static void* mt_count(void* a_) {
+  mt_part_arg* a = (mt_part_arg*)a_;
+  for (uint64_t i = a->lo; i < a->hi; i++) a->cnt[(uint64_t)((uint32_t)a->in[i].val % a->np) * a->nt + a->t]++;
+  return NULL;
+}
+
+static void* mt_scatter(void* a_) {
+  mt_part_arg* a = (mt_part_arg*)a_;
+  for (uint64_t i = a->lo; i < a->hi; i++) {
+    uint64_t* pos = &a->cnt[(uint64_t)((uint32_t)a->in[i].val % a->np) * a->nt + a->t];
+    a->out[(*pos)++] = a->in[i];
+  }
+  return NULL;
+}
+
+/* partition one side with nt threads; start[p] = first row of partition p */
+static int mt_partition(const ejo_tuple* in, uint64_t n, uint32_t np, uint32_t nt, ejo_tuple* out,
+                        uint64_t* start) {
+  uint64_t* cnt = (uint64_t*)calloc((size_t)np * nt, sizeof(uint64_t));
+  mt_part_arg* args = (mt_part_arg*)calloc(nt, sizeof(mt_part_arg));
+  pthread_t* th = (pthread_t*)calloc(nt, sizeof(pthread_t));
+  if (!cnt || !args || !th) { free(cnt); free(args); free(th); return -1; }
+  const uint64_t chunk = (n + nt - 1) / nt;
+  for (uint32_t t = 0; t < nt; t++) {
+    args[t].in = in; args[t].n = n; args[t].np = np; args[t].t = t; args[t].nt = nt;
+    args[t].cnt = cnt; args[t].out = out;
+    args[t].lo = (uint64_t)t * chunk < n ? (uint64_t)t * chunk : n;
+    args[t].hi = args[t].lo + chunk < n ? args[t].lo + chunk : n;
+  }
+  for (uint32_t t = 0; t < nt; t++) pthread_create(&th[t], NULL, mt_count, &args[t]);
+  for (uint32_t t = 0; t < nt; t++) pthread_join(th[t], NULL);
+  uint64_t run = 0;
+  for (uint64_t k = 0; k < (uint64_t)np * nt; k++) {
+    const uint64_t c = cnt[k];
+    cnt[k] = run;
+    run += c;
+  }
+  for (uint32_t p = 0; p < np; p++) start[p] = cnt[(uint64_t)p * nt];
+  start[np] = n;
+  for (uint32_t t = 0; t < nt; t++) pthread_create(&th[t], NULL, mt_scatter, &args[t]);
+  for (uint32_t t = 0; t < nt; t++) pthread_join(th[t], NULL);
+  free(cnt); free(args); free(th);
+  return 0;
+}
+
+typedef struct {
+  const ejo_tuple *pr, *ps;
+  const uint64_t *rstart, *sstart;
+  uint32_t np;
+  uint32_t* next;        /* shared partition counter */
+  uint64_t* pcount;      /* matches of each partition (first pass) */
+  const uint64_t* poff;  /* output offset of each partition (second pass) */
+  ejo_result* out;
+  uint64_t cap;
+} mt_join_arg;
+
+/* threads take partitions from the shared counter; first pass: count each
+ * partition's matches, second pass (poff set): write them at its offset */
+static void* mt_join(void* a_) {
+  mt_join_arg* a = (mt_join_arg*)a_;
+  for (;;) {
+    const uint32_t p = __atomic_fetch_add(a->next, 1u, __ATOMIC_RELAXED);
+    if (p >= a->np) break;
+    uint64_t n = a->poff ? a->poff[p] : 0;
+    for (uint64_t i = a->sstart[p]; i < a->sstart[p + 1]; i++) {
+      const ejo_tuple* s = &a->ps[i];
+      for (uint64_t j = a->rstart[p]; j < a->rstart[p + 1]; j++) {
+        const ejo_tuple* r = &a->pr[j];
+        if (s->val != r->val) continue;
+        if (a->poff) emit(a->out, a->cap, n, r, s);
+        n++;
+      }
+    }
+    if (!a->poff) a->pcount[p] = n;
+  }
+  return NULL;
+}
+
+static void mt_run(mt_join_arg* args, pthread_t* th, uint32_t nthreads) {
+  uint32_t next = 0;
+  for (uint32_t t = 0; t < nthreads; t++) {
+    args[t].next = &next;
+    pthread_create(&th[t], NULL, mt_join, &args[t]);
+  }
+  for (uint32_t t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+}
+
+uint64_t ejo_hash_join_mt(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS,
+                          ejo_result* out, uint64_t cap, uint32_t partitions, uint32_t nthreads) {
+  if (partitions == 0) partitions = 1u << 17;
+  if (nthreads == 0) nthreads = 8;
+  ejo_tuple* pr = (ejo_tuple*)malloc(sizeof(ejo_tuple) * (nR ? nR : 1));
+  ejo_tuple* ps = (ejo_tuple*)malloc(sizeof(ejo_tuple) * (nS ? nS : 1));
+  uint64_t* rstart = (uint64_t*)malloc(sizeof(uint64_t) * ((uint64_t)partitions + 1));
+  uint64_t* sstart = (uint64_t*)malloc(sizeof(uint64_t) * ((uint64_t)partitions + 1));
+  uint64_t* pcount = (uint64_t*)malloc(sizeof(uint64_t) * partitions);
+  uint64_t* poff = (uint64_t*)malloc(sizeof(uint64_t) * partitions);
+  mt_join_arg* args = (mt_join_arg*)calloc(nthreads, sizeof(mt_join_arg));
+  pthread_t* th = (pthread_t*)calloc(nthreads, sizeof(pthread_t));
+  uint64_t total = UINT64_MAX;
+  if (!pr || !ps || !rstart || !sstart || !pcount || !poff || !args || !th) goto done;
+  if (mt_partition(R, nR, partitions, nthreads, pr, rstart) || mt_partition(S, nS, partitions, nthreads, ps, sstart))
+    goto done;
+  for (uint32_t t = 0; t < nthreads; t++) {
+    args[t].pr = pr; args[t].ps = ps; args[t].rstart = rstart; args[t].sstart = sstart;
+    args[t].np = partitions; args[t].pcount = pcount; args[t].out = out; args[t].cap = cap;
+  }
+  mt_run(args, th, nthreads);
+  total = 0;
+  for (uint32_t p = 0; p < partitions; p++) {
+    poff[p] = total;
+    total += pcount[p];
+  }
+  if (out && cap) {
+    for (uint32_t t = 0; t < nthreads; t++) args[t].poff = poff;
+    mt_run(args, th, nthreads);
+  }
+done:
+  free(pr); free(ps); free(rstart); free(sstart); free(pcount); free(poff); free(args); free(th);
+  return total;
 }
 
 /* ---------------------------------------------------------------------------

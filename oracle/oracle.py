@@ -25,7 +25,7 @@ def build(force: bool = False) -> str:
             os.path.getmtime(LIB) >= os.path.getmtime(p) for p in (SRC, GEN_H)):
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-ffp-contract=off", "-I",
+    cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-I",
            os.path.join(ROOT, "include"), SRC, "-o", LIB + ".tmp", "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(LIB + ".tmp", LIB)
@@ -47,6 +47,8 @@ def load() -> C.CDLL:
         for name in ("ejo_sort_index_join", "ejo_bnl_join"):
             getattr(lib, name).argtypes = [vp, u64, vp, u64, vp, u64]
             getattr(lib, name).restype = u64
+        lib.ejo_hash_join_mt.argtypes = [vp, u64, vp, u64, vp, u64, u32, u32]
+        lib.ejo_hash_join_mt.restype = u64
         lib.ejo_hash_join_count.argtypes = [vp, u64, vp, u64, u32]
         lib.ejo_hash_join_count.restype = u64
         lib.ejo_star_join3.argtypes = [vp, vp, u64, vp, u64, vp, u64, vp, u64, u32]
@@ -107,6 +109,20 @@ def _join(name: str, R, S, extra=()) -> np.ndarray:
 def hash_join(R, S, nb_bktent: int = 1 << 20) -> np.ndarray:
     """joins/CPU_JOIN/hash_cpu restated (partitioned hash join)."""
     return _join("ejo_hash_join", R, S, (nb_bktent,))
+
+
+def hash_join_mt(R, S, threads: int = 0, partitions: int = 1 << 17) -> np.ndarray:
+    """joins/multi_joins/hash restated (pthread partitioned hash join); threads 0: every host core."""
+    lib = load()
+    R, S = _rel(R), _rel(S)
+    nt = threads or os.cpu_count() or 8
+    n = int(lib.ejo_hash_join_mt(_p(R), len(R), _p(S), len(S), None, 0, partitions, nt))
+    out = np.empty((max(n, 1), 4), dtype=np.int32)
+    m = int(lib.ejo_hash_join_mt(_p(R), len(R), _p(S), len(S), _p(out), n, partitions, nt))
+    if m == 2 ** 64 - 1:
+        raise MemoryError("ejo_hash_join_mt")
+    assert m == n
+    return out[:n]
 
 
 def hash_index_join(R, S, nb_bucket: int = 1 << 20) -> np.ndarray:

@@ -127,3 +127,19 @@ def test_checksum_order_independent():
     rows2 = rows.copy()
     rows2[5, 2] ^= 1
     assert O.checksum(rows) != O.checksum(rows2)
+
+
+@pytest.mark.parametrize("threads,partitions", [(1, 1 << 17), (4, 1 << 10), (7, 3)])
+def test_multithreaded_restatement(threads, partitions):
+    """joins/multi_joins/hash restated with pthreads: the same multiset as the
+    single-threaded hash_cpu restatement, and the join_ori known answer."""
+    rng = np.random.default_rng(threads)
+    for nR, nS, lo, hi in ((0, 10, 0, 5), (10, 0, 0, 5), (1000, 5000, -2 ** 31, 2 ** 31 - 1),
+                           (3, 100000, 0, 4), (12345, 54321, -1000, 1000)):
+        R = np.stack([np.arange(nR), rng.integers(lo, hi, nR)], 1).astype(np.int32).reshape(-1, 2)
+        S = np.stack([np.arange(nS), rng.integers(lo, hi, nS)], 1).astype(np.int32).reshape(-1, 2)
+        got = O.hash_join_mt(R, S, threads=threads, partitions=partitions)
+        assert np.array_equal(O.canon(got), O.canon(O.hash_join(R, S)))
+    R, S = golden.join_ori()
+    rows = O.hash_join_mt(R, S, threads=threads, partitions=partitions)
+    assert len(rows) == 1002230 and int(rows[:, 1].astype(np.int64).sum()) == 50438235
