@@ -402,6 +402,32 @@ def run_configs(steps: int) -> None:
     lines.append({"config": "C4 star join F=2^26 x D1, D2 = 2^20", "ms": round(ms, 4), "rows": n,
                   "tuples_per_s": (2 * t["F1"].shape[0] + nd) / (ms / 1000),
                   "roofline": hbm(8 * nd + 16 * t["F1"].shape[0] + 32 * n, ms)})
+    # distance joins: all 2^38 pairs of 2^19 x 2^19 reference-shaped points, radius 1
+    from eating_one_gb300.native import point_result_dtype
+    from eating_one_gb300.workloads import distance_workload
+    from oracle import oracle as O
+
+    fp32 = props.multi_processor_count * 128 * 2.07e9  # one FP32 lane-instruction per clock per lane
+    for name in ("d2", "d3"):
+        dims, Rp, Sp = distance_workload(name)
+        dR, dS = eng.points_to_device(Rp), eng.points_to_device(Sp)
+        n = eng.distance_join_count(dR, dS, dims)
+        out = torch.empty((n, point_result_dtype(dims).itemsize), dtype=torch.uint8, device="cuda")
+        ms = timed(lambda: eng.distance_join(dR, dS, dims, 1.0, out=out), max(3, steps // 4))
+        pairs = len(Rp) * len(Sp)
+        # CPU: the oracle restatement on every host core, over a bounded slice of S
+        threads = os.cpu_count() or 1
+        s_sample = Sp[:1024]
+        t0 = time.perf_counter()
+        O.distance_join(dims, Rp, s_sample, 1.0, threads=threads)
+        cpu_s = time.perf_counter() - t0
+        lines.append({"config": "%dD distance join R=2^19 x S=2^19 points, radius 1, 10%% copies" % dims,
+                      "ms": round(ms, 4), "rows": n, "pairs_per_s": pairs / (ms / 1000),
+                      "roofline": {"bound": "fp32 issue", "peak_lane_ops_per_s": fp32,
+                                   "frac_at_two_ops_per_pair": round(2 * pairs / (ms / 1000) / fp32, 4)},
+                      "cpu_baseline": {"pairs_per_s": len(Rp) * len(s_sample) / cpu_s, "cores": threads,
+                                       "kind": "port", "sample": "R=2^19 x the first 1024 S points"},
+                      "reference_cpu_log": "2-D 2^19 x 2^19 in 3718 s (complex_block/2d_cpu/nohup.out)"})
     for ln in lines:
         print(json.dumps(ln), flush=True)
 
@@ -421,7 +447,7 @@ def main() -> None:
     ap.add_argument("--requests", type=int, default=10000)
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--lanes", type=int, default=2)
-    ap.add_argument("--configs", action="store_true", help="time configurations C1, C2 and C4 instead")
+    ap.add_argument("--configs", action="store_true", help="time configurations C1, C2, C4 and the 2-D/3-D distance joins instead")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.configs:

@@ -195,6 +195,47 @@ class Engine:
             self.h, _ptr(F1), _ptr(F2), F1.shape[0], _ptr(D1), D1.shape[0], _ptr(D2), D2.shape[0], o, cap, cnt),
             out, 8)
 
+    # ---- distance joins -------------------------------------------------------------
+    def points_to_device(self, points) -> torch.Tensor:
+        """A numpy array of native.point_dtype(dims) as a (n, point bytes) uint8 device tensor."""
+        import numpy as np
+        raw = np.ascontiguousarray(points).view(np.uint8).reshape(len(points), points.dtype.itemsize)
+        return torch.from_numpy(raw).to(self.device)
+
+    @staticmethod
+    def rows_to_numpy(rows: torch.Tensor, dims: int):
+        """Distance-join rows (uint8 tensor) as a numpy array of native.point_result_dtype(dims)."""
+        return rows.cpu().contiguous().numpy().reshape(-1).view(native.point_result_dtype(dims))
+
+    def distance_join(self, R: torch.Tensor, S: torch.Tensor, dims: int, radius: float = 1.0,
+                      out: torch.Tensor | None = None) -> torch.Tensor:
+        """Distance nested-loop join of device point arrays (see points_to_device): S point l
+        and R point r match when sum_i (r.val[i] - l.val[i])^2 < radius^2.  Returns a
+        (count, row bytes) uint8 tensor of native.point_result_dtype(dims) rows."""
+        pb, rb = native.point_dtype(dims).itemsize, native.point_result_dtype(dims).itemsize
+        nR, nS = R.numel() // pb, S.numel() // pb
+        self._sync_stream()
+        cnt = C.c_uint64(0)
+        if out is None:
+            self._check(self.lib.ej_distance_join_count(self.h, dims, _ptr(R), nR, _ptr(S), nS, radius,
+                                                        C.byref(cnt)))
+            out = torch.empty((cnt.value, rb), dtype=torch.uint8, device=self.device)
+            if cnt.value == 0:
+                return out
+        st = self._check(self.lib.ej_distance_join(self.h, dims, _ptr(R), nR, _ptr(S), nS, radius, _ptr(out),
+                                                   out.shape[0], C.byref(cnt)), allow_capacity=True)
+        if st == native.EJ_ERR_CAPACITY:
+            raise JoinError(st, "%d results do not fit the %d-row output" % (cnt.value, out.shape[0]))
+        return out[: cnt.value]
+
+    def distance_join_count(self, R: torch.Tensor, S: torch.Tensor, dims: int, radius: float = 1.0) -> int:
+        pb = native.point_dtype(dims).itemsize
+        self._sync_stream()
+        cnt = C.c_uint64(0)
+        self._check(self.lib.ej_distance_join_count(self.h, dims, _ptr(R), R.numel() // pb, _ptr(S),
+                                                    S.numel() // pb, radius, C.byref(cnt)))
+        return cnt.value
+
     def build_index(self, kind: str, R: torch.Tensor) -> Index:
         self._sync_stream()
         ix = C.c_void_p()

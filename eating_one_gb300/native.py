@@ -27,6 +27,30 @@ ALGO = {"hash": 0, "single_hash": 1, "bnl": 2, "hash_index": 3, "sort_index": 4,
 EJ_GEN_PERM, EJ_GEN_UNIFORM, EJ_GEN_ZIPF = 0, 1, 2
 
 
+def _np():
+    import numpy as np
+    return np
+
+
+def point_dtype(dims: int):
+    """numpy dtype of ej_point2 / ej_point3: {int32 id; double val[dims]} (24 or 32 bytes)."""
+    np = _np()
+    if dims not in (2, 3):
+        raise ValueError("dims must be 2 or 3")
+    return np.dtype([("id", "<i4"), ("val", "<f8", (dims,))], align=True)
+
+
+def point_result_dtype(dims: int):
+    """numpy dtype of ej_point_result2 {lid, lval[2], rid, rval[2]} (48 bytes) or
+    ej_point_result3 {lval[3], rval[3], lid, rid} (56 bytes)."""
+    np = _np()
+    if dims == 2:
+        return np.dtype([("lid", "<i4"), ("lval", "<f8", (2,)), ("rid", "<i4"), ("rval", "<f8", (2,))], align=True)
+    if dims == 3:
+        return np.dtype([("lval", "<f8", (3,)), ("rval", "<f8", (3,)), ("lid", "<i4"), ("rid", "<i4")], align=True)
+    raise ValueError("dims must be 2 or 3")
+
+
 class GenSpec(C.Structure):
     """Mirror of ej_gen_spec (include/ej_gen.h)."""
 
@@ -102,6 +126,8 @@ _SIGS = {
     "ej_single_hash_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_bnl_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_bnl_join_count": [_vp, _vp, _u64, _vp, _u64, _pu64],
+    "ej_distance_join": [_vp, C.c_uint32, _vp, _u64, _vp, _u64, C.c_double, _vp, _u64, _pu64],
+    "ej_distance_join_count": [_vp, C.c_uint32, _vp, _u64, _vp, _u64, C.c_double, _pu64],
     "ej_hash_index_build": [_vp, _vp, _u64, C.POINTER(C.c_void_p)],
     "ej_sort_index_build": [_vp, _vp, _u64, C.POINTER(C.c_void_p)],
     "ej_index_free": [_vp, _vp],

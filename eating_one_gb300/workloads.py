@@ -79,6 +79,56 @@ def workload(name: str, scale: int = 0) -> dict[str, GenSpec]:
     raise KeyError(name)
 
 
+# distance joins: the reference's logged 2-D runs go up to 2^19 x 2^19 points
+# (joins/blockJoin_gpu/complex_block/2d_cpu/nohup.out)
+DIST_WORKLOADS = {"d2": (2, 19), "d3": (3, 19)}
+
+
+def distance_workload(name: str, scale: int = 0, seed: int | None = None):
+    """(dims, R, S) of a named distance workload: |R| = |S| = 2^(log2 - scale)."""
+    dims, lg = DIST_WORKLOADS[name]
+    n = 1 << (lg - scale)
+    return (dims,) + distance_points(dims, n, n, SEED_BASE + 16 + dims if seed is None else seed)
+
+
+def distance_points(dims: int, n_right: int, n_left: int, seed: int, match_rate: float = 0.1,
+                    selectivity: int = 1000000000):
+    """Seeded points shaped as the reference's distance-join generator
+    (joins/CPU_JOIN/3d_cpu/nestLoopJoin.cc:114-186): every point has one
+    integer value in [0, selectivity) in all dimensions, unique over both
+    relations, except that every l_diff-th left point (l_diff = n_left /
+    (match_rate n_right)) copies the values of a distinct random right point
+    until ceil(match_rate n_right) have been copied.  Ids count from 1, right
+    points first.  Returns (R, S) as numpy arrays of native.point_dtype(dims)."""
+    import math
+
+    import numpy as np
+
+    from .native import point_dtype
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    need = n_right + n_left
+    vals = np.empty(0, dtype=np.int64)
+    while len(vals) < need:
+        draw = np.unique(np.concatenate([vals, rng.integers(0, selectivity, size=need + need // 16 + 64)]))
+        vals = draw
+    vals = rng.permutation(vals)[:need].astype(np.float64)
+    R = np.zeros(n_right, dtype=point_dtype(dims))
+    S = np.zeros(n_left, dtype=point_dtype(dims))
+    R["id"] = np.arange(1, n_right + 1, dtype=np.int32)
+    S["id"] = np.arange(n_right + 1, n_right + n_left + 1, dtype=np.int32)
+    rv = vals[:n_right]
+    lv = vals[n_right:].copy()
+    if match_rate > 0 and n_right and n_left:
+        l_diff = max(1, int(n_left / (match_rate * n_right)))
+        pos = np.arange(0, n_left, l_diff)[: math.ceil(match_rate * n_right)]
+        pos = pos[: n_right]
+        lv[pos] = rv[rng.choice(n_right, size=len(pos), replace=False)]
+    R["val"] = rv[:, None]
+    S["val"] = lv[:, None]
+    return R, S
+
+
 def alg_bytes(name: str, n_r: int, n_s: int, n_out: int) -> int:
     """Algorithmic bytes of one join (roofline numerator).
 

@@ -51,6 +51,15 @@ typedef struct ej_result { int32_t rkey; int32_t rval; int32_t lkey; int32_t lva
 /* one row of the 3-way star join: the two binary result rows of one fact row */
 typedef struct ej_star_result { ej_result d1; ej_result d2; } ej_star_result;
 
+/* points and result rows of the distance joins, laid out as the reference's:
+ * the 2-D GPU join's TUPLE and JOIN_TUPLE (joins/blockJoin_gpu/complex_block/
+ * dire_join/tuple.h:20-30, 24 and 48 bytes) and the 3-D CPU join's
+ * (joins/CPU_JOIN/3d_cpu/nestLoopJoin.cc:23-33, 32 and 56 bytes) */
+typedef struct ej_point2 { int32_t id; double val[2]; } ej_point2;
+typedef struct ej_point3 { int32_t id; double val[3]; } ej_point3;
+typedef struct ej_point_result2 { int32_t lid; double lval[2]; int32_t rid; double rval[2]; } ej_point_result2;
+typedef struct ej_point_result3 { double lval[3]; double rval[3]; int32_t lid; int32_t rid; } ej_point_result3;
+
 typedef enum ej_status {
   EJ_OK = 0,
   EJ_ERR_INVALID = 1,   /* bad argument (null pointer, size out of range) */
@@ -163,6 +172,19 @@ ej_status ej_bnl_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tup
                       ej_result* out, uint64_t out_cap, uint64_t* out_count);
 ej_status ej_bnl_join_count(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
                             uint64_t nS, uint64_t* out_count);
+
+/* Distance nested-loop join over all |R|x|S| point pairs: S point l (left)
+ * and R point r (right) match when sum_i (r.val[i] - l.val[i])^2 < radius^2,
+ * evaluated in IEEE double in the reference's order (eval of
+ * joins/blockJoin_gpu/complex_block/dire_join/join_gpu.cu:12-26 with its
+ * count/join kernels :30-130, and of joins/CPU_JOIN/3d_cpu/nestLoopJoin.cc:73-101;
+ * radius = DISTANCE = 1 there).  dims is 2 (R, S are ej_point2, out is
+ * ej_point_result2) or 3 (ej_point3, ej_point_result3); arrays are device
+ * memory, 8-byte aligned.  Rows come in no particular order. */
+ej_status ej_distance_join(ej_handle* h, uint32_t dims, const void* R, uint64_t nR, const void* S, uint64_t nS,
+                           double radius, void* out, uint64_t out_cap, uint64_t* out_count);
+ej_status ej_distance_join_count(ej_handle* h, uint32_t dims, const void* R, uint64_t nR, const void* S,
+                                 uint64_t nS, double radius, uint64_t* out_count);
 
 /* ---- index joins ---------------------------------------------------------- */
 

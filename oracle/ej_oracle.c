@@ -487,6 +487,126 @@ uint64_t ejo_hash_join_count(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S
 }
 
 /* ---------------------------------------------------------------------------
+ * Distance nested-loop join: joins/CPU_JOIN/3d_cpu/nestLoopJoin.cc:73-101
+ * (VAL_NUM 3) and joins/blockJoin_gpu/complex_block/2d_cpu/nestLoopJoin.cc:73-101
+ * (VAL_NUM 2): every left (S) point against every right (R) point, left-major;
+ * eval computes t = r.val[i] - l.val[i], temp += t * t in double and matches
+ * on temp < radius * radius (DISTANCE = 1 there).  This file is compiled with
+ * -ffp-contract=off, so every operation rounds on its own as in the reference.
+ * Rows: dims 2 {lid; lval[2]; rid; rval[2]} (blockJoin_gpu/complex_block/
+ * dire_join/tuple.h:25-30), dims 3 {lval[3]; rval[3]; lid; rid}
+ * (3d_cpu/nestLoopJoin.cc:28-33); padding bytes are zero.
+ * nthreads > 1 splits S into contiguous ranges, counts each, then writes each
+ * at its offset: the rows come out in the single-threaded order.
+ * ------------------------------------------------------------------------- */
+typedef struct { int32_t lid; double lval[2]; int32_t rid; double rval[2]; } ejo_point_result2;
+typedef struct { double lval[3]; double rval[3]; int32_t lid, rid; } ejo_point_result3;
+
+static size_t dist_point_bytes(uint32_t dims) { return 8 + 8 * (size_t)dims; }
+static int32_t dist_id(const char* p) { int32_t id; memcpy(&id, p, 4); return id; }
+static const double* dist_val(const char* p) { return (const double*)(p + 8); }
+
+static int dist_eval(const double* r, const double* l, uint32_t dims, double r2) {
+  double temp = 0, t;
+  for (uint32_t i = 0; i < dims; i++) {
+    t = r[i] - l[i];
+    temp += t * t;
+  }
+  return temp < r2;
+}
+
+static void dist_emit(void* out, uint64_t n, uint32_t dims, const char* l, const char* r) {
+  const double* lv = dist_val(l);
+  const double* rv = dist_val(r);
+  if (dims == 2) {
+    ejo_point_result2 row;
+    memset(&row, 0, sizeof row);
+    row.lid = dist_id(l);
+    row.rid = dist_id(r);
+    for (int i = 0; i < 2; i++) { row.lval[i] = lv[i]; row.rval[i] = rv[i]; }
+    memcpy((char*)out + n * sizeof row, &row, sizeof row);
+  } else {
+    ejo_point_result3 row;
+    memset(&row, 0, sizeof row);
+    row.lid = dist_id(l);
+    row.rid = dist_id(r);
+    for (int i = 0; i < 3; i++) { row.lval[i] = lv[i]; row.rval[i] = rv[i]; }
+    memcpy((char*)out + n * sizeof row, &row, sizeof row);
+  }
+}
+
+typedef struct {
+  uint32_t dims;
+  const char *R, *S;
+  uint64_t nR, s0, s1;
+  double r2;
+  void* out;     /* NULL: count only */
+  uint64_t base; /* first row of this range */
+  uint64_t cap;
+  uint64_t n;
+} dist_arg;
+
+static void* dist_range(void* a_) {
+  dist_arg* a = (dist_arg*)a_;
+  const size_t pb = dist_point_bytes(a->dims);
+  uint64_t n = 0;
+  for (uint64_t i = a->s0; i < a->s1; i++) {
+    const char* l = a->S + i * pb;
+    for (uint64_t j = 0; j < a->nR; j++) {
+      const char* r = a->R + j * pb;
+      if (dist_eval(dist_val(r), dist_val(l), a->dims, a->r2)) {
+        if (a->out && a->base + n < a->cap) dist_emit(a->out, a->base + n, a->dims, l, r);
+        n++;
+      }
+    }
+  }
+  a->n = n;
+  return NULL;
+}
+
+uint64_t ejo_distance_join(uint32_t dims, const void* R, uint64_t nR, const void* S, uint64_t nS, double radius,
+                           void* out, uint64_t cap, uint32_t nthreads) {
+  if (dims != 2 && dims != 3) return UINT64_MAX;
+  if (nthreads == 0) nthreads = 1;
+  if ((uint64_t)nthreads > nS) nthreads = nS ? (uint32_t)nS : 1;
+  dist_arg* args = (dist_arg*)calloc(nthreads, sizeof(dist_arg));
+  pthread_t* th = (pthread_t*)calloc(nthreads, sizeof(pthread_t));
+  if (!args || !th) { free(args); free(th); return UINT64_MAX; }
+  const double r2 = radius * radius;
+  for (uint32_t t = 0; t < nthreads; t++) {
+    dist_arg* a = &args[t];
+    a->dims = dims;
+    a->R = (const char*)R;
+    a->S = (const char*)S;
+    a->nR = nR;
+    a->s0 = nS * t / nthreads;
+    a->s1 = nS * (t + 1) / nthreads;
+    a->r2 = r2;
+  }
+  /* pass 1: counts; pass 2 (rows wanted): each range at its offset */
+  for (int pass = 0; pass < (out ? 2 : 1); pass++) {
+    uint64_t base = 0;
+    for (uint32_t t = 0; t < nthreads; t++) {
+      args[t].out = pass ? out : NULL;
+      args[t].cap = cap;
+      args[t].base = base;
+      base += args[t].n;
+    }
+    if (nthreads == 1) {
+      dist_range(&args[0]);
+    } else {
+      for (uint32_t t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, dist_range, &args[t]);
+      for (uint32_t t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    }
+  }
+  uint64_t n = 0;
+  for (uint32_t t = 0; t < nthreads; t++) n += args[t].n;
+  free(args);
+  free(th);
+  return n;
+}
+
+/* ---------------------------------------------------------------------------
  * Inputs and result canonicalisation
  * ------------------------------------------------------------------------- */
 void ejo_generate(const ej_gen_spec* sp, ejo_tuple* out) {

@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the bench's
 CPU-baseline leg as the checker.  The join engine never imports this module.
 Arrays are numpy int32: relations (n, 2) = TUPLE{key, val}, results (n, 4) =
-RESULT{rkey, rval, lkey, lval}, star results (n, 8).
+RESULT{rkey, rval, lkey, lval}, star results (n, 8).  Distance joins take and
+return numpy structured arrays (POINT_DTYPE, POINT_RESULT_DTYPE).
 """
 from __future__ import annotations
 
@@ -59,6 +60,8 @@ def load() -> C.CDLL:
         lib.ejo_canon_sort_star.argtypes = [vp, u64]
         lib.ejo_checksum.argtypes = [vp, u64, u32]
         lib.ejo_checksum.restype = u64
+        lib.ejo_distance_join.argtypes = [u32, vp, u64, vp, u64, C.c_double, vp, u64, u32]
+        lib.ejo_distance_join.restype = u64
         _lib = lib
     return _lib
 
@@ -177,3 +180,54 @@ def checksum(rows: np.ndarray) -> int:
     """Order-independent 64-bit checksum (sum of a per-row mix), as ej_checksum computes."""
     rows = np.ascontiguousarray(rows, dtype=np.int32)
     return int(load().ejo_checksum(_p(rows), len(rows), rows.shape[1] if rows.ndim == 2 else 4))
+
+
+# ---- distance joins ------------------------------------------------------------
+# TUPLE {int id; double val[dims]}; rows as the reference lays them out: dims 2
+# {lid, lval[2], rid, rval[2]} (blockJoin_gpu/complex_block/dire_join/tuple.h:25-30),
+# dims 3 {lval[3], rval[3], lid, rid} (CPU_JOIN/3d_cpu/nestLoopJoin.cc:28-33)
+POINT_DTYPE = {d: np.dtype([("id", "<i4"), ("val", "<f8", (d,))], align=True) for d in (2, 3)}
+POINT_RESULT_DTYPE = {
+    2: np.dtype([("lid", "<i4"), ("lval", "<f8", (2,)), ("rid", "<i4"), ("rval", "<f8", (2,))], align=True),
+    3: np.dtype([("lval", "<f8", (3,)), ("rval", "<f8", (3,)), ("lid", "<i4"), ("rid", "<i4")], align=True),
+}
+# the 2-D CPU program's row (joins/blockJoin_gpu/complex_block/2d_cpu/nestLoopJoin.cc:28-33)
+REF_CPU_ROW2_DTYPE = np.dtype([("lval", "<f8", (2,)), ("rval", "<f8", (2,)), ("lid", "<i4"), ("rid", "<i4")])
+
+
+def distance_join(dims: int, R, S, radius: float = 1.0, threads: int = 1) -> np.ndarray:
+    """CPU_JOIN/3d_cpu (dims 3) / complex_block/2d_cpu (dims 2) restated: every
+    (S, R) pair with sum_i (r.val[i] - l.val[i])^2 < radius^2, left-major order."""
+    lib = load()
+    R = np.ascontiguousarray(R, dtype=POINT_DTYPE[dims])
+    S = np.ascontiguousarray(S, dtype=POINT_DTYPE[dims])
+    n = int(lib.ejo_distance_join(dims, _p(R), len(R), _p(S), len(S), radius, None, 0, threads))
+    if n == 2 ** 64 - 1:
+        raise MemoryError("ejo_distance_join")
+    out = np.zeros(max(n, 1), dtype=POINT_RESULT_DTYPE[dims])
+    m = int(lib.ejo_distance_join(dims, _p(R), len(R), _p(S), len(S), radius, out.ctypes.data, n, threads))
+    assert m == n
+    return out[:n]
+
+
+def point_rows_canon(rows: np.ndarray) -> np.ndarray:
+    """Distance-join rows of any of the layouts as an int64 matrix
+    [lid, rid, lval bits..., rval bits...] in lexicographic order: equal
+    matrices mean the same rows, bit for bit."""
+    rows = np.asarray(rows)
+    d = rows.dtype["lval"].shape[0]
+    m = np.empty((len(rows), 2 + 2 * d), dtype=np.int64)
+    m[:, 0] = rows["lid"]
+    m[:, 1] = rows["rid"]
+    m[:, 2:2 + d] = np.ascontiguousarray(rows["lval"]).view(np.int64).reshape(-1, d)
+    m[:, 2 + d:] = np.ascontiguousarray(rows["rval"]).view(np.int64).reshape(-1, d)
+    if len(m):
+        m = m[np.lexsort(m.T[::-1])]
+    return m
+
+
+def point_rows_digest(rows: np.ndarray) -> str:
+    """sha256 of point_rows_canon(rows)."""
+    import hashlib
+
+    return hashlib.sha256(point_rows_canon(rows).tobytes()).hexdigest()

@@ -19,13 +19,24 @@
 // R/S files use the reference's table format: int32 count, then TUPLE[count]
 // (joins/hashJoin_gpu/main_street/TableBuild.cpp:118-140).  The program is run
 // as `<prog> |S| |R|` (left = S = argv[1], right = R = argv[2]).
+//
+// EJ_REF_TUPLE_BYTES and EJ_REF_ROW_BYTES give the program's TUPLE and result
+// row sizes: 8 and 16 for the equi-joins (the default), 32 and 56 for the 3-D
+// distance join (joins/CPU_JOIN/3d_cpu/nestLoopJoin.cc:23-33), 24 and 40 for
+// the 2-D one (joins/blockJoin_gpu/complex_block/2d_cpu/nestLoopJoin.cc).
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
+#ifndef EJ_REF_TUPLE_BYTES
+#define EJ_REF_TUPLE_BYTES 8
+#endif
+#ifndef EJ_REF_ROW_BYTES
+#define EJ_REF_ROW_BYTES 16
+#endif
+
 struct ej_ref_tuple {
-  int key;
-  int val;
+  unsigned char bytes[EJ_REF_TUPLE_BYTES];
 };
 
 // the reference's globals (unmangled: namespace-scope variables)
@@ -61,15 +72,20 @@ extern "C" void ej_ref_free(void* p) {
   }
 #ifdef EJ_REF_RESULT
   if (g_dump && p && p == EJ_REF_RESULT) {
-    // result rows are 16 bytes; the array was calloc'ed, and every row holds a
-    // nonzero row id (ids start at 1 in the dumped tables), so the first
-    // all-zero row ends the written prefix
-    const int* w = static_cast<const int*>(p);
+    // the result array was calloc'ed, and every row holds a nonzero row id
+    // (ids start at 1 in the dumped tables), so the first all-zero row ends
+    // the written prefix
+    const unsigned char* w = static_cast<const unsigned char*>(p);
     FILE* f = fopen(g_dump, "wb");
     const long max_rows = strtol(getenv("EJ_REF_DUMP_MAX") ? getenv("EJ_REF_DUMP_MAX") : "67108864", nullptr, 10);
     long n = 0;
-    while (n < max_rows && (w[4 * n] | w[4 * n + 1] | w[4 * n + 2] | w[4 * n + 3])) n++;
-    fwrite(w, 16, n, f);
+    for (; n < max_rows; n++) {
+      const unsigned char* row = w + (size_t)n * EJ_REF_ROW_BYTES;
+      int nonzero = 0;
+      for (int b = 0; b < EJ_REF_ROW_BYTES; b++) nonzero |= row[b];
+      if (!nonzero) break;
+    }
+    fwrite(w, EJ_REF_ROW_BYTES, n, f);
     fclose(f);
   }
 #endif

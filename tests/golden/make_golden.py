@@ -14,6 +14,14 @@ Run in a checkout that has the reference at $EJ_REFERENCE (default
    oracle/ref_shim.cpp; the match count each prints and, where the program
    materialises rows, the order-independent checksum of those rows (mapped to
    RESULT{rkey, rval, lkey, lval} with r = right/R) are recorded.
+3. Distance joins: the unmodified joins/CPU_JOIN/3d_cpu and
+   joins/blockJoin_gpu/complex_block/2d_cpu programs (radius DISTANCE = 1) are
+   fed points the same way: reference-shaped inputs (integer values, 10%
+   copies) and boundary cases (tests.golden.boundary_points).  The inputs go
+   to distance.npz, the printed count and the sha256 of the canonical rows
+   (oracle.point_rows_digest) to reference_runs.json["distance"].
+
+`--distance-only` redoes part 3 alone and keeps the rest of reference_runs.json.
 """
 from __future__ import annotations
 
@@ -31,8 +39,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from eating_one_gb300.workloads import workload  # noqa: E402
+from eating_one_gb300.workloads import distance_points, workload  # noqa: E402
 from oracle import oracle as O  # noqa: E402
+from tests.golden import boundary_points  # noqa: E402
 
 REF = os.environ.get("EJ_REFERENCE", "/root/reference")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref")
@@ -88,8 +97,61 @@ def run_cpu_join(prog: str, R: np.ndarray, S: np.ndarray):
         return count, rows, diffs, out
 
 
+# (case, dims, generator): radius 1, the reference programs' DISTANCE
+DIST_CASES = [
+    ("ref_shape_2d", 2, lambda: distance_points(2, 1000, 1500, 0xD157_0002)),
+    ("ref_shape_3d", 3, lambda: distance_points(3, 1000, 1500, 0xD157_0003)),
+    ("boundary_2d", 2, lambda: boundary_points(2, 600, 800, 0xB0_0002)),
+    ("boundary_3d", 3, lambda: boundary_points(3, 600, 800, 0xB0_0003)),
+]
+
+
+def write_points(path: str, P: np.ndarray) -> None:
+    with open(path, "wb") as f:
+        np.array([len(P)], dtype=np.int32).tofile(f)
+        f.write(np.ascontiguousarray(P).tobytes())
+
+
+def run_distance(dims: int, R: np.ndarray, S: np.ndarray):
+    prog = os.path.join(REF_BIN, "dist%d_cpu" % dims)
+    with tempfile.TemporaryDirectory() as tmp:
+        rp, sp, dp = (os.path.join(tmp, x) for x in ("R.pts", "S.pts", "rows.bin"))
+        write_points(rp, R)
+        write_points(sp, S)
+        out = subprocess.run([prog, rp, sp, dp], cwd=tmp, check=True, stdout=subprocess.PIPE, text=True).stdout
+        # init() prints the generator's copy count, join() the match count
+        count = int(re.findall(r"^(\d+)$", out, re.M)[-1])
+        row = O.POINT_RESULT_DTYPE[3] if dims == 3 else O.REF_CPU_ROW2_DTYPE
+        rows = np.fromfile(dp, dtype=row) if os.path.exists(dp) else np.zeros(0, dtype=row)
+        return count, rows
+
+
+def distance_runs() -> list:
+    arrays, runs = {}, []
+    for case, dims, gen in DIST_CASES:
+        R, S = gen()
+        count, rows = run_distance(dims, R, S)
+        assert len(rows) == count, (case, len(rows), count)
+        digest = O.point_rows_digest(rows)
+        mine = O.distance_join(dims, R, S)
+        assert O.point_rows_digest(mine) == digest, case + ": the oracle differs from the reference"
+        arrays[case + "_R"] = np.ascontiguousarray(R).view(np.uint8)
+        arrays[case + "_S"] = np.ascontiguousarray(S).view(np.uint8)
+        runs.append({"case": case, "dims": dims, "nR": len(R), "nS": len(S), "count": count, "digest": digest})
+        print(case, count, digest[:16])
+    np.savez_compressed(os.path.join(HERE, "distance.npz"), **arrays)
+    return runs
+
+
 def main() -> None:
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    if "--distance-only" in sys.argv:
+        with open(os.path.join(HERE, "reference_runs.json")) as f:
+            runs = json.load(f)
+        runs["distance"] = distance_runs()
+        with open(os.path.join(HERE, "reference_runs.json"), "w") as f:
+            json.dump(runs, f, indent=1)
+        return
     runs: dict = {"join_ori": {}, "cpu_join": []}
 
     # 1. join_ori fixture
@@ -121,6 +183,7 @@ def main() -> None:
         runs["cpu_join"].append(entry)
         print(prog, name, scale, count, entry["checksum"], diffs)
 
+    runs["distance"] = distance_runs()
     with open(os.path.join(HERE, "reference_runs.json"), "w") as f:
         json.dump(runs, f, indent=1)
     print(json.dumps(runs["join_ori"]))
