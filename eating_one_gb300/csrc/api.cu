@@ -92,6 +92,7 @@ extern "C" ej_status ej_destroy(ej_handle* h) {
   if (!h) return EJ_ERR_INVALID;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  ej_stream_release(h);
   cudaFree(h->arena);
   cudaFree(h->stage);
   cudaFree(h->d_status);
@@ -118,6 +119,7 @@ extern "C" ej_status ej_trim(ej_handle* h) {
   if (!h) return EJ_ERR_INVALID;
   EJ_CUDA(h, cudaSetDevice(h->device));
   EJ_CUDA(h, cudaStreamSynchronize(h->stream));
+  ej_stream_release(h);
   EJ_CUDA(h, cudaFree(h->arena));
   EJ_CUDA(h, cudaFree(h->stage));
   h->arena = h->stage = nullptr;

@@ -204,18 +204,17 @@ bnl_kernel(const ej_tuple* __restrict__ R, uint64_t nR, const ej_tuple* __restri
 
 template <bool USE_TMA, bool COUNT_ONLY>
 ej_status launch_bnl(ej_handle* h, dim3 grid, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
-                     uint64_t s_per_cta, ej_result* out, uint64_t cap) {
+                     uint64_t s_per_cta, ej_result* out, uint64_t cap, unsigned long long* cursor) {
   auto k = bnl_kernel<USE_TMA, COUNT_ONLY>;
   EJ_CUDA(h, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BnSmem)));
-  k<<<grid, BN_THREADS, sizeof(BnSmem), h->stream>>>(R, nR, S, nS, s_per_cta, out, cap, h->d_words, h->d_status);
+  k<<<grid, BN_THREADS, sizeof(BnSmem), h->stream>>>(R, nR, S, nS, s_per_cta, out, cap, cursor, h->d_status);
   return ej_check_launch(h, "bnl_kernel");
 }
 
-}  // namespace
-
-static ej_status bnl_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
-                         ej_result* out, uint64_t cap, bool count_only) {
-  EJ_CUDA(h, cudaMemsetAsync(h->d_words, 0, sizeof(unsigned long long), h->stream));
+// the nested loop over R x S; rows go to out at the positions *cursor hands
+// out (not reset here, so successive calls append)
+ej_status bnl_launch(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                     ej_result* out, uint64_t cap, bool count_only, unsigned long long* cursor) {
   if (nR == 0 || nS == 0) return EJ_OK;
   const uint64_t rchunks = (nR + BN_RCHUNK - 1) / BN_RCHUNK;
   if (rchunks > 0x7FFFFFFFull) return ej_fail(h, EJ_ERR_TOO_LARGE, "R too large for the nested loop");
@@ -231,18 +230,29 @@ static ej_status bnl_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_
   splits = (nS + s_per_cta - 1) / s_per_cta;
   const dim3 grid((unsigned)rchunks, (unsigned)splits);
   const bool tma = ((uintptr_t)S % 16) == 0;
+  if (count_only)
+    return tma ? launch_bnl<true, true>(h, grid, R, nR, S, nS, s_per_cta, out, cap, cursor)
+               : launch_bnl<false, true>(h, grid, R, nR, S, nS, s_per_cta, out, cap, cursor);
+  return tma ? launch_bnl<true, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap, cursor)
+             : launch_bnl<false, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap, cursor);
+}
+
+}  // namespace
+
+static ej_status bnl_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                         ej_result* out, uint64_t cap, bool count_only) {
+  EJ_CUDA(h, cudaMemsetAsync(h->d_words, 0, sizeof(unsigned long long), h->stream));
   // one pass: the whole nested loop is recorded as the write phase
   ej_phase_begin(h);
   for (int k = 1; k < EJ_PHASES; k++) ej_phase_mark(h, k);
-  ej_status st;
-  if (count_only)
-    st = tma ? launch_bnl<true, true>(h, grid, R, nR, S, nS, s_per_cta, out, cap)
-             : launch_bnl<false, true>(h, grid, R, nR, S, nS, s_per_cta, out, cap);
-  else
-    st = tma ? launch_bnl<true, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap)
-             : launch_bnl<false, false>(h, grid, R, nR, S, nS, s_per_cta, out, cap);
+  const ej_status st = bnl_launch(h, R, nR, S, nS, out, cap, count_only, h->d_words);
   ej_phase_mark(h, EJ_PHASES);
   return st;
+}
+
+ej_status ej_bnl_append(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                        ej_result* out, uint64_t cap, unsigned long long* cursor) {
+  return bnl_launch(h, R, nR, S, nS, out, cap, false, cursor);
 }
 
 extern "C" ej_status ej_bnl_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,

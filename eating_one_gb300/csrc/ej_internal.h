@@ -54,6 +54,8 @@ struct ej_handle {
   // host-buffer entry points: device staging owned separately from the arena
   void* stage = nullptr;
   size_t stage_cap = 0;
+  // chunked host-buffer joins: copy streams, events, device and pinned buffers
+  struct ej_stream_res* sres = nullptr;
   // synchronous batched joins: per-join counts
   unsigned long long* d_batch_counts = nullptr;
   unsigned long long* h_batch_counts = nullptr;
@@ -71,6 +73,12 @@ struct ej_plan_bytes {
 };
 
 ej_status ej_fail(ej_handle* h, ej_status s, const char* fmt, ...);
+// frees the chunked-join resources (stream_join.cu); safe on a handle without them
+void ej_stream_release(ej_handle* h);
+// block nested loop over R x S (bnlj.cu); rows go to out at positions taken
+// from *cursor, which is not reset, so successive calls append
+ej_status ej_bnl_append(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
+                        ej_result* out, uint64_t cap, unsigned long long* cursor);
 ej_status ej_arena_reserve(ej_handle* h, size_t bytes);
 inline char* ej_arena_at(ej_handle* h, size_t off) { return static_cast<char*>(h->arena) + off; }
 ej_status ej_check_launch(ej_handle* h, const char* what);

@@ -254,6 +254,20 @@ class Engine:
         self._check(st, allow_capacity=True)
         return cnt.value
 
+    def join_host_chunked(self, algo: str, R, S, out, r_block: int = 0, s_chunk: int = 0) -> int:
+        """Out-of-core host-buffer join ("hash" or "bnl"): R in device blocks of r_block rows, S
+        streamed in chunks of s_chunk rows (0: sized by the library).  Returns the count; rows
+        copied: min(count, len(out)).  Pinned host tensors are used in place."""
+        def p(a):
+            return a.ctypes.data if hasattr(a, "ctypes") else a.data_ptr()
+        self._sync_stream()
+        cfg = native.ChunkConfig(r_block, s_chunk)
+        cnt = C.c_uint64(0)
+        st = self.lib.ej_join_host_chunked(self.h, native.ALGO[algo], p(R), len(R), p(S), len(S), p(out),
+                                           len(out), C.byref(cnt), C.byref(cfg))
+        self._check(st, allow_capacity=True)
+        return cnt.value
+
     # ---- utilities ----------------------------------------------------------------
     def exclusive_scan_u32(self, x: torch.Tensor) -> torch.Tensor:
         self._sync_stream()

@@ -92,6 +92,10 @@ class Completion(C.Structure):
                 ("arrival_ns", C.c_uint64), ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64)]
 
 
+class ChunkConfig(C.Structure):
+    _fields_ = [("r_block_rows", C.c_uint64), ("s_chunk_rows", C.c_uint64)]
+
+
 class TuneEntry(C.Structure):
     """Mirror of ej_tune_entry (include/ej.h)."""
 
@@ -148,6 +152,7 @@ _SIGS = {
     "ej_server_destroy": [_vp],
     "ej_now_ns": [],
     "ej_join_host": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
+    "ej_join_host_chunked": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64, _vp],
     "ej_exclusive_scan_u32": [_vp, _vp, _u64, _vp],
     "ej_exclusive_scan_u32_noalloc": [_vp, _u64, _vp, _vp],
     "ej_generate": [_vp, C.POINTER(GenSpec), _vp],

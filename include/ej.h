@@ -310,6 +310,26 @@ ej_status ej_join_host(ej_handle* h, ej_algo algo, const ej_tuple* R, uint64_t n
                        const ej_tuple* S, uint64_t nS, ej_result* out, uint64_t out_cap,
                        uint64_t* out_count);
 
+/* Out-of-core form of ej_join_host for the hash join (EJ_ALGO_HASH) and the
+ * block nested loop (EJ_ALGO_BNL): relations and result of any size.  R goes
+ * to the device in blocks of at most r_block_rows (the hash join builds each
+ * block's table once); S streams through in chunks of at most s_chunk_rows,
+ * double-buffered, so the upload of one chunk and the download of the
+ * previous chunk's rows overlap the join of the current one.  Pinned host
+ * buffers are used in place (a pinned out receives rows straight from the
+ * write pass); pageable ones are staged.  Rows come in (R block, S chunk)
+ * order; past out_cap they are counted only (EJ_ERR_CAPACITY, *out_count =
+ * the full count).  Replaces the whole-relation transfers around the
+ * reference kernels (joins/hashJoin_gpu/main_street/hj.cc:345-354, :1124) and
+ * the device-sized tiling of joins/blockJoin_gpu/main_street/nestLoopJoin.cc:326-519. */
+typedef struct ej_chunk_config {
+  uint64_t r_block_rows; /* 0: sized from the free device memory */
+  uint64_t s_chunk_rows; /* 0: 2^25 rows */
+} ej_chunk_config;
+ej_status ej_join_host_chunked(ej_handle* h, ej_algo algo, const ej_tuple* R, uint64_t nR,
+                               const ej_tuple* S, uint64_t nS, ej_result* out, uint64_t out_cap,
+                               uint64_t* out_count, const ej_chunk_config* cfg);
+
 /* ---- prefix scan ----------------------------------------------------------- */
 
 /* Exclusive prefix sum of n uint32 counts into n+1 uint64 offsets (out[n] =
