@@ -11,9 +11,10 @@ every input is far larger than the 126 MB L2).
 
 Printed (rank 0, one JSON line):
   value      input tuples/s of the whole job (all ranks), inputs resident in HBM
-  e2e        the same metric through ej_join_host (the C ABI call with host
-             buffers: host->device copies of R and S and the device->host copy
-             of every result row inside the timed region)
+  e2e        the same metric through ej_join_host_chunked (the C ABI call with
+             host buffers: host->device copies of R and S and the device->host
+             transfer of every result row inside the timed region), with the
+             CPU-GPU link's measured bandwidth and the floor it sets
   roofline   the dominant kernel's algorithmic bytes / its event-timed duration
   join_roofline  algorithmic bytes of the whole join, 24(|R|+|S|) + 16|out|,
              over the step time - the fraction of the HBM roofline
@@ -111,6 +112,42 @@ class ClockSampler:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def link_bandwidth(pinned) -> dict:
+    """CPU-GPU link: pinned host-to-device, device-to-host and both at once
+    (GB/s), copies of up to 1 GiB between `pinned` (a pinned host tensor) and
+    device memory, best of three."""
+    import torch
+
+    nbytes = min(pinned.numel() * pinned.element_size(), 1 << 30) // 2
+    host = pinned.view(-1).view(torch.uint8)[: 2 * nbytes]
+    dev = torch.empty(2 * nbytes, dtype=torch.uint8, device="cuda")
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def best(fn):
+        t = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            t.append(time.perf_counter() - t0)
+        return min(t)
+
+    def h2d():
+        with torch.cuda.stream(up):
+            dev[:nbytes].copy_(host[:nbytes], non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(down):
+            host[nbytes:].copy_(dev[nbytes:], non_blocking=True)
+
+    t_up, t_down = best(h2d), best(d2h)
+    t_both = best(lambda: (h2d(), d2h()))
+    del dev
+    return {"h2d_gbs": round(nbytes / t_up / 1e9, 1), "d2h_gbs": round(nbytes / t_down / 1e9, 1),
+            "both_gbs": round(nbytes / t_both / 1e9, 1)}
 
 
 def dist_setup():
@@ -566,23 +603,27 @@ def main() -> None:
         out_h = torch.empty((max_out, 4), dtype=torch.int32, pin_memory=True)
         for j in joins:
             hosts.append((j["R"].cpu().pin_memory(), j["S"].cpu().pin_memory(), j["n_out"]))
-        eng.join_host("hash", hosts[0][0], hosts[0][1], out_h)  # warm-up
+        eng.join_host_chunked("hash", hosts[0][0], hosts[0][1], out_h)  # warm-up
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             for Rh, Sh, n_out in hosts:
-                n = eng.join_host("hash", Rh, Sh, out_h)
+                n = eng.join_host_chunked("hash", Rh, Sh, out_h)
                 assert n == n_out
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        link = link_bandwidth(out_h)
         if dist:
             t = torch.tensor([e2e_s], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_s = float(t.item())
-        e2e = {"value": units * world / e2e_s, "unit": UNIT,
-               "h2d_bytes_per_step": int(sum(8 * (R.shape[0] + S.shape[0]) for R, S, _ in hosts)),
-               "d2h_bytes_per_step": int(sum(16 * n for _, _, n in hosts)),
-               "ms_per_step": round(e2e_s * 1000.0, 3)}
+        h2d = int(sum(8 * (R.shape[0] + S.shape[0]) for R, S, _ in hosts))
+        d2h = int(sum(16 * n for _, _, n in hosts))
+        e2e = {"value": units * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": round(e2e_s * 1000.0, 3),
+               "api": "ej_join_host_chunked (pinned host R, S and out; 2^25-row S chunks)",
+               "link": dict(link, floor_ms=round(1000.0 * max(h2d / (link["both_gbs"] * 1e9),
+                                                               d2h / (link["both_gbs"] * 1e9)), 2))}
 
     if rank != 0:
         if dist:

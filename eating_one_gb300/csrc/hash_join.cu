@@ -260,7 +260,7 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
   const ej_tuple* P = S;
   if (L.pb) {
     ej_tuple* spart = reinterpret_cast<ej_tuple*>(ej_arena_at(h, L.spart_off));
-    EJ_TRY(ej_radix_pass(h, L.splan, S, spart, 32u - L.pb, L.pb));
+    EJ_TRY(ej_partition_pass(h, L.splan, S, spart, 32u - L.pb, L.pb));
     P = spart;
   }
   ej_phase_mark(h, 2);

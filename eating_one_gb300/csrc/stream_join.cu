@@ -220,7 +220,7 @@ ej_status sj_hash_begin(ej_handle* h, ej_stream_res* r, Job& j, const ej_tuple* 
   c.P = Sd;
   if (c.L.pb) {
     ej_tuple* spart = reinterpret_cast<ej_tuple*>(ej_arena_at(h, c.L.spart_off));
-    EJ_TRY(ej_radix_pass(h, c.L.splan, Sd, spart, 32u - c.L.pb, c.L.pb));
+    EJ_TRY(ej_partition_pass(h, c.L.splan, Sd, spart, 32u - c.L.pb, c.L.pb));
     c.P = spart;
   }
   EJ_TRY(ej_probe_count(h, c.L.pp, c.P, j.t, false, h->d_words + 1));
