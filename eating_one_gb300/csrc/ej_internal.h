@@ -144,9 +144,11 @@ void ej_radix_plan_add(ej_plan_bytes& p, ej_radix_plan& rp, uint64_t n);
 ej_status ej_radix_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
                         uint32_t shift, uint32_t bits, int digit_kind = EJ_DIGIT_HASH);
 // the same pass writing keys and vals to two arrays (last pass of a table build)
-// one-pass partition by a hash digit, order within a partition unspecified
+// a pass whose order within a digit is unspecified: a one-pass partition, or
+// the first pass of an LSD sort (the later, stable passes decide every order
+// that matters)
 ej_status ej_partition_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
-                            uint32_t shift, uint32_t bits);
+                            uint32_t shift, uint32_t bits, int digit_kind = EJ_DIGIT_HASH);
 ej_status ej_radix_pass_soa(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, int32_t* out_keys,
                             int32_t* out_vals, uint32_t shift, uint32_t bits, int digit_kind);
 

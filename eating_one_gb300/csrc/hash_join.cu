@@ -146,7 +146,10 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
     if (p + 1 == tp.passes) {
       EJ_TRY(ej_radix_pass_soa(h, tp.rplan, src, rkey, rval, shift, 8u, digit_kind));
     } else {
-      EJ_TRY(ej_radix_pass(h, tp.rplan, src, tmp[p & 1], shift, 8u, digit_kind));
+      if (p == 0)
+        EJ_TRY(ej_partition_pass(h, tp.rplan, src, tmp[0], shift, 8u, digit_kind));
+      else
+        EJ_TRY(ej_radix_pass(h, tp.rplan, src, tmp[p & 1], shift, 8u, digit_kind));
       src = tmp[p & 1];
     }
   }

@@ -91,14 +91,36 @@ __device__ __forceinline__ unsigned long long ej_group_rows(uint32_t c, uint32_t
   return __shfl_sync(EJ_FULL_MASK, incl, 31);
 }
 
-// keys of the first PW_PREFETCH rows of every run
+// keys of the first PW_PREFETCH rows of every run: the aligned 8-key window
+// holding them, in one or two 16-byte loads (rkey - voff is 16-byte aligned
+// and the column is padded, so the window stays inside it)
 __device__ __forceinline__ void ej_probe_prefetch(const ej_table_view& t, const EjProbeWarp& w,
                                                   int32_t (&kk)[PR_ITEMS][PW_PREFETCH]) {
+  static_assert(PW_PREFETCH == 4, "the window holds 4 keys past any offset");
+  const int4* rk4 = reinterpret_cast<const int4*>(t.rkey - t.voff);
+  int4 qa[PR_ITEMS], qb[PR_ITEMS];
+  uint32_t o[PR_ITEMS];
 #pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++)
+  for (int j = 0; j < PR_ITEMS; j++) {
+    qa[j] = qb[j] = make_int4(EJ_NULL_KEY, EJ_NULL_KEY, EJ_NULL_KEY, EJ_NULL_KEY);
+    o[j] = 0;
+    if (w.lo[j] != NULL_RUN && w.cnt[j]) {
+      const uint32_t p = w.lo[j] + t.voff;
+      o[j] = p & 3u;
+      qa[j] = __ldg(rk4 + p / 4);
+      if (o[j] + min(w.cnt[j], (uint32_t)PW_PREFETCH) > 4u) qb[j] = __ldg(rk4 + p / 4 + 1);
+    }
+  }
 #pragma unroll
-    for (int e = 0; e < PW_PREFETCH; e++)
-      kk[j][e] = (w.lo[j] != NULL_RUN && (uint32_t)e < w.cnt[j]) ? __ldg(t.rkey + w.lo[j] + e) : EJ_NULL_KEY;
+  for (int j = 0; j < PR_ITEMS; j++) {
+    const int32_t x[8] = {qa[j].x, qa[j].y, qa[j].z, qa[j].w, qb[j].x, qb[j].y, qb[j].z, qb[j].w};
+#pragma unroll
+    for (int e = 0; e < PW_PREFETCH; e++) {
+      // x[o + e] with static indices only
+      const int32_t v = o[j] == 0 ? x[e] : o[j] == 1 ? x[e + 1] : o[j] == 2 ? x[e + 2] : x[e + 3];
+      kk[j][e] = (uint32_t)e < w.cnt[j] ? v : EJ_NULL_KEY;
+    }
+  }
 }
 
 // group rows of one lane: buffer rows [r, r + c), keys from kk for the first

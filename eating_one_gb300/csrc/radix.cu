@@ -264,8 +264,10 @@ ej_status ej_radix_pass_soa(ej_handle* h, const ej_radix_plan& rp, const ej_tupl
 }
 
 ej_status ej_partition_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
-                            uint32_t shift, uint32_t bits) {
+                            uint32_t shift, uint32_t bits, int digit_kind) {
   if (rp.n == 0) return EJ_OK;
   EJ_TRY(check_digit(h, shift, bits));
+  if (digit_kind == EJ_DIGIT_VALUE)
+    return radix_pass_kind<EJ_DIGIT_VALUE, false, false>(h, rp, in, out, nullptr, nullptr, shift, bits);
   return radix_pass_kind<EJ_DIGIT_HASH, false, false>(h, rp, in, out, nullptr, nullptr, shift, bits);
 }
