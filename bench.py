@@ -274,7 +274,9 @@ def run_reference(args) -> None:
 
 def run_profile_case(name: str, scale: int, repeat: int) -> None:
     """A small case for profilers: `repeat` hash joins of one workload at
-    1/2^scale size, each synchronised; prints the phase times of the last."""
+    1/2^scale size, each synchronised; prints the phase times of the last.
+    d2 / d3: `repeat` distance joins of 2^(19 - scale) x 2^(19 - scale) points
+    (after one count-only call)."""
     import torch
 
     from eating_one_gb300.build import build
@@ -283,6 +285,19 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
 
     build()
     eng = Engine(0)
+    if name in ("d2", "d3"):  # distance joins: dist_screen_kernel x2 + dist_kernel per call
+        from eating_one_gb300.native import point_result_dtype
+        from eating_one_gb300.workloads import distance_workload
+
+        dims, Rp, Sp = distance_workload(name, scale)
+        dR, dS = eng.points_to_device(Rp), eng.points_to_device(Sp)
+        n_out = eng.distance_join_count(dR, dS, dims)
+        out = torch.empty((n_out, point_result_dtype(dims).itemsize), dtype=torch.uint8, device="cuda")
+        for _ in range(repeat):
+            assert eng.distance_join(dR, dS, dims, 1.0, out=out).shape[0] == n_out
+        print(json.dumps({"profile_case": name, "scale": scale, "R": len(Rp), "S": len(Sp), "rows": n_out}),
+              flush=True)
+        return
     w = workload(name, scale)
     R, S = eng.generate(w["R"]), eng.generate(w["S"])
     n_out = eng.count("hash", R, S)

@@ -27,15 +27,21 @@
 // __dadd_rn in the reference's order: no fused multiply-add), so the matches
 // are the reference's, bit for bit.
 //
-// Layout: each CTA holds x of 4096 R points in registers (16 per thread); the
-// x of S stream through shared memory in 4096-point tiles.  The test of one
-// pair is one float subtraction and one compare-and-accumulate.  Matches take
-// an output slot from an atomic cursor (the row order is not deterministic,
-// the row multiset is); count-only mode sums per-thread counters.
+// Layout: each CTA holds x of 16384 R points in registers (64 per thread,
+// packed in pairs; 160 registers, one CTA per SM, which the pure arithmetic
+// loop needs no more than); the x of S stream through shared memory in
+// 4096-point tiles.  Per S point a
+// thread takes the smallest (x_s - x_r)^2 over its 16 R points with packed
+// two-lane subtractions and products and three-input minima (three
+// instructions per two pairs) and compares it with W^2 once; only then are
+// the slots tested one by one.  Matches take an output slot from an atomic cursor (the row order is
+// not deterministic, the row multiset is); count-only mode sums per-thread
+// counters.
 #include <float.h>
 #include <math.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "ej_device.cuh"
 #include "ej_entry.h"
@@ -43,7 +49,7 @@
 namespace {
 
 constexpr int DJ_THREADS = 256;
-constexpr int DJ_RK = 16;                      // R points per thread
+constexpr int DJ_RK = 64;                      // R points per thread
 constexpr int DJ_RCHUNK = DJ_THREADS * DJ_RK;  // R points per CTA
 constexpr int DJ_STILE = 4096;                 // S screen values per shared-memory tile (16 KB)
 
@@ -70,6 +76,25 @@ __device__ __forceinline__ float dist_clamp(float x) {
 __device__ __forceinline__ float dist_bound(float rad_up, float m_s, float m_r) {
   const float err = __fmul_ru(0x1p-24f, __fadd_ru(m_s, m_r));
   return __fmul_ru(__fadd_ru(__fadd_ru(rad_up, err), 0x1p-148f), 1.0f + 0x1p-23f);
+}
+
+// two float differences in one instruction (Blackwell packed f32x2):
+// (x - lo(r), x - hi(r)) for x2 = (x, x), each rounded to nearest like __fsub_rn
+__device__ __forceinline__ unsigned long long dist_sub2(unsigned long long x2, unsigned long long r) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(x2), "l"(r));
+  return d;
+}
+
+// minimum of three floats in one instruction; NaN operands are ignored
+__device__ __forceinline__ float dist_min3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+__device__ __forceinline__ unsigned long long dist_pack(float lo, float hi) {
+  return (unsigned long long)__float_as_uint(hi) << 32 | __float_as_uint(lo);
 }
 
 // block-wide maximum (NaN inputs ignored); every thread gets it
@@ -141,19 +166,25 @@ dist_kernel(const Point<D>* __restrict__ R, const float* __restrict__ rx_all, ui
   __shared__ float red[DJ_THREADS / 32];
   __shared__ unsigned long long warp_tmp[DJ_THREADS / 32 + 1];
   const uint64_t rbase = (uint64_t)blockIdx.x * DJ_RCHUNK;
-  float rx[DJ_RK];
-  uint32_t valid = 0;
+  // the thread's R screen values in pairs, for the packed subtraction
+  unsigned long long rx2[DJ_RK / 2];
+  using Mask = typename std::conditional<(DJ_RK > 32), unsigned long long, uint32_t>::type;
+  Mask valid = 0;
   float m = 0.0f;
 #pragma unroll
-  for (int k = 0; k < DJ_RK; k++) {
-    const uint64_t ri = rbase + (uint64_t)k * DJ_THREADS + threadIdx.x;
-    float x = __int_as_float(0x7fc00000);  // slots past nR: NaN, never a candidate
-    if (ri < nR) {
-      x = __ldg(rx_all + ri);
-      valid |= 1u << k;
+  for (int k = 0; k < DJ_RK; k += 2) {
+    float x[2];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const uint64_t ri = rbase + (uint64_t)(k + e) * DJ_THREADS + threadIdx.x;
+      x[e] = __int_as_float(0x7fc00000);  // slots past nR: NaN, never a candidate
+      if (ri < nR) {
+        x[e] = __ldg(rx_all + ri);
+        valid |= (Mask)1 << (k + e);
+      }
+      m = fmaxf(m, fabsf(x[e]));
     }
-    m = fmaxf(m, fabsf(x));
-    rx[k] = dist_clamp(x);
+    rx2[k / 2] = dist_pack(dist_clamp(x[0]), dist_clamp(x[1]));
   }
   const float m_r = dist_block_max(m, red);
   const uint64_t s_begin = (uint64_t)blockIdx.y * s_per_cta;
@@ -172,18 +203,28 @@ dist_kernel(const Point<D>* __restrict__ R, const float* __restrict__ rx_all, ui
     if (!valid) continue;
     for (uint32_t k = 0; k < n; k++) {
       const float xs = tile[k];
-      bool cand = false;
+      // the smallest |xs - x_r| over the thread's R points (NaN differences
+      // ignored): two differences per instruction, two minima per instruction
+      const unsigned long long xs2 = dist_pack(xs, xs);
+      float dmin = INFINITY;
 #pragma unroll
-      for (int j = 0; j < DJ_RK; j++) cand |= fabsf(__fsub_rn(xs, rx[j])) <= W;
-      if (!cand) continue;
-      // the rare path: candidate slots as a bit mask (static indices keep rx in registers)
-      uint32_t mask = 0;
+      for (int j = 0; j < DJ_RK / 2; j++) {
+        const unsigned long long d = dist_sub2(xs2, rx2[j]);
+        dmin = dist_min3(dmin, fabsf(__uint_as_float((uint32_t)d)), fabsf(__uint_as_float((uint32_t)(d >> 32))));
+      }
+      if (!(dmin <= W)) continue;
+      // the rare path: candidate slots as a bit mask (static indices keep rx2 in registers)
+      Mask mask = 0;
 #pragma unroll
-      for (int j = 0; j < DJ_RK; j++) mask |= (uint32_t)(fabsf(__fsub_rn(xs, rx[j])) <= W) << j;
+      for (int j = 0; j < DJ_RK / 2; j++) {
+        const unsigned long long d = dist_sub2(xs2, rx2[j]);
+        mask |= (Mask)(fabsf(__uint_as_float((uint32_t)d)) <= W) << (2 * j);
+        mask |= (Mask)(fabsf(__uint_as_float((uint32_t)(d >> 32))) <= W) << (2 * j + 1);
+      }
       mask &= valid;
       const Point<D> l = S[t0 + k];
       for (; mask; mask &= mask - 1) {
-        const int j = __ffs(mask) - 1;
+        const int j = DJ_RK > 32 ? __ffsll((long long)mask) - 1 : __ffs((int)mask) - 1;
         const Point<D> r = R[rbase + (uint64_t)j * DJ_THREADS + threadIdx.x];
         if (!dist_match<D>(r, l, r2)) continue;
         if (COUNT_ONLY) {
