@@ -167,7 +167,9 @@ struct ej_table_view {
   int kind = EJ_TABLE_HASH;
   const int32_t* rkey = nullptr;     // [nR + pad] row ids in table order
   const int32_t* rval = nullptr;     // [nR + pad] join keys in table order
-  const uint2* bucket = nullptr;     // [2^hb] (hash): row bounds of each bucket
+  const uint2* bucket = nullptr;     // [2^hb] (hash, batched tables): row bounds of each bucket
+  const uint4* dir = nullptr;        // (hash, single tables) key directory {hash, start, length, 0}
+  const uint32_t* dir_bits = nullptr;  // device word: the directory has 2^bits home slots
   const int32_t* fence = nullptr;    // [nfence] (sorted)
   uint64_t nR = 0;
   uint32_t hb = 1;

@@ -29,6 +29,8 @@
 //          probe order, then R run order.
 // The same kernels serve the sort index (runs by binary search) and the left
 // outer join (OUTER: a probe without matches yields one NULL-extended row).
+#include <climits>
+
 #include "ej_device.cuh"
 #include "hash_join.cuh"
 #include "probe.cuh"
@@ -37,13 +39,218 @@
 namespace {
 
 
-// Row bounds of every bucket of the hash-sorted table: row i (i = nR: the
-// end) begins the buckets between the bucket of row i - 1 and its own; each
-// warp takes 256 consecutive rows.
-__global__ void __launch_bounds__(256)
-bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb) {
-  const uint64_t r0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * 256;
-  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket);
+// ---- key directory of a hash table ----------------------------------------
+// The distinct keys of the hash-sorted table, in hash order, each an entry
+// {hash, run start, run length, 0} placed by linear probing from its home slot
+// hash >> (32 - bits), 2^bits >= 2 x keys: key k goes to
+//   pos_k = max(home_k, pos_{k-1} + 1) = k + max_{j <= k} (home_j - j),
+// so the entries stay in hash order and a probe walks forward from its home
+// slot past smaller hashes until it meets its hash, a larger one or an empty
+// slot (length 0).  Each key also writes the empty slots between its
+// predecessor's entry and its own; dir_edge_kernel empties the slots before
+// the first entry and after the last (up to 2^bits, and one past the last
+// entry).  The number of keys, and so bits, is known only on the device: it
+// lives in the header in front of the entries.  Build: per 4096-row tile,
+// count the rows that begin a key; scan; per tile, the key starts and the
+// largest home_k - k; a prefix maximum over the tiles; per tile, the entries.
+
+constexpr int DIR_ROWS = 16;              // consecutive rows per thread
+constexpr int DIR_TILE = 256 * DIR_ROWS;  // rows per block
+
+struct DirHeader {
+  uint32_t bits;
+  uint32_t pad;
+  unsigned long long nkeys;
+  unsigned long long pos_first, pos_last;  // slots of the first and last entries
+};
+constexpr size_t DIR_HEADER_BYTES = 256;
+
+// DIR_ROWS consecutive rows of a thread: vals and which of them begin a key
+struct DirRows {
+  int32_t v[DIR_ROWS];
+  uint32_t f;  // bit e: row i0 + e begins a key
+};
+
+__device__ __forceinline__ void dir_rows(const int32_t* __restrict__ rval, uint64_t n, uint64_t i0, DirRows& r) {
+  r.f = 0;
+#pragma unroll
+  for (int e = 0; e < DIR_ROWS; e++) r.v[e] = 0;
+  if (i0 >= n) return;
+  // i0 is a multiple of DIR_ROWS; the column is 16-byte aligned and padded by
+  // 8 rows, so the vector loads past n that can happen stay inside it
+#pragma unroll
+  for (int q = 0; q < DIR_ROWS / 4; q++) {
+    if (i0 + 4u * q >= n) break;
+    const int4 x = *reinterpret_cast<const int4*>(rval + i0 + 4u * q);
+    r.v[4 * q] = x.x;
+    r.v[4 * q + 1] = x.y;
+    r.v[4 * q + 2] = x.z;
+    r.v[4 * q + 3] = x.w;
+  }
+  int32_t prev = i0 ? rval[i0 - 1] : 0;
+#pragma unroll
+  for (int e = 0; e < DIR_ROWS; e++) {
+    if (i0 + e < n && (i0 + e == 0 || r.v[e] != prev)) r.f |= 1u << e;
+    prev = r.v[e];
+  }
+}
+
+__device__ __forceinline__ uint32_t dir_bits_for(unsigned long long nk) {
+  uint32_t bits = 1;
+  while (bits < 32 && (1ull << bits) < 2 * nk) bits++;
+  return bits;
+}
+
+// block-wide maximum scan, exclusive (LLONG_MIN for thread 0); *total = the block maximum
+__device__ __forceinline__ long long dir_block_exclusive_max(long long v, long long* tmp, long long* total) {
+  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (unsigned)o) incl = max(incl, u);
+  }
+  if (lane == 31u) tmp[warp] = incl;
+  __syncthreads();
+  long long before = LLONG_MIN;
+  for (unsigned w = 0; w < warp; w++) before = max(before, tmp[w]);
+  long long all = LLONG_MIN;
+  for (unsigned w = 0; w < nw; w++) all = max(all, tmp[w]);
+  const long long up = __shfl_up_sync(0xffffffffu, incl, 1);
+  const long long ex = max(before, lane ? up : LLONG_MIN);
+  __syncthreads();
+  *total = all;
+  return ex;
+}
+
+// rows beginning a key, per tile
+__global__ void __launch_bounds__(256) dir_count_kernel(const int32_t* __restrict__ rval, uint64_t n,
+                                                        uint32_t* __restrict__ tile_keys) {
+  __shared__ uint32_t tmp[256 / 32 + 1];
+  DirRows r;
+  dir_rows(rval, n, (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS, r);
+  uint32_t total;
+  ej_block_exclusive_sum<256, uint32_t>((uint32_t)__popc(r.f), tmp, &total);
+  if (threadIdx.x == 0) tile_keys[blockIdx.x] = total;
+}
+
+// per tile: the start row of each of its keys (starts[nkeys] = n) and the
+// largest home_k - k; the header's key count and bits
+__global__ void __launch_bounds__(256) dir_compact_kernel(const int32_t* __restrict__ rval, uint64_t n,
+                                                          const uint32_t* __restrict__ tile_off, uint32_t ntiles,
+                                                          uint32_t* __restrict__ starts, long long* __restrict__ kmax,
+                                                          DirHeader* hdr) {
+  __shared__ uint32_t tmp[256 / 32 + 1];
+  __shared__ long long tmpl[256 / 32];
+  const uint64_t i0 = (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS;
+  DirRows r;
+  dir_rows(rval, n, i0, r);
+  uint32_t total;
+  uint64_t k = tile_off[blockIdx.x] + ej_block_exclusive_sum<256, uint32_t>((uint32_t)__popc(r.f), tmp, &total);
+  const unsigned long long nk = tile_off[ntiles];
+  const uint32_t shift = 32u - dir_bits_for(nk);
+  long long m = LLONG_MIN;
+#pragma unroll
+  for (int e = 0; e < DIR_ROWS; e++)
+    if (r.f >> e & 1u) {
+      starts[k] = (uint32_t)(i0 + e);
+      m = max(m, (long long)(ej_hash32((uint32_t)r.v[e]) >> shift) - (long long)k);
+      k++;
+    }
+  long long all;
+  dir_block_exclusive_max(m, tmpl, &all);
+  if (threadIdx.x == 0) kmax[blockIdx.x] = all;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    starts[nk] = (uint32_t)n;
+    hdr->bits = 32u - shift;
+    hdr->nkeys = nk;
+  }
+}
+
+// exclusive prefix maximum over the tiles (one block)
+__global__ void __launch_bounds__(1024) dir_prefix_kernel(const long long* __restrict__ kmax, uint32_t ntiles,
+                                                          long long* __restrict__ kpre) {
+  __shared__ long long tmp[1024 / 32];
+  const uint64_t per = (ntiles + blockDim.x - 1) / blockDim.x;
+  const uint64_t c0 = min((uint64_t)ntiles, threadIdx.x * per), c1 = min((uint64_t)ntiles, c0 + per);
+  long long m = LLONG_MIN;
+  for (uint64_t c = c0; c < c1; c += 8) {  // eight independent loads in flight
+    long long x[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) x[u] = c + u < c1 ? kmax[c + u] : LLONG_MIN;
+#pragma unroll
+    for (int u = 0; u < 8; u++) m = max(m, x[u]);
+  }
+  long long all;
+  long long run = dir_block_exclusive_max(m, tmp, &all);
+  for (uint64_t c = c0; c < c1; c += 8) {
+    long long x[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) x[u] = c + u < c1 ? kmax[c + u] : LLONG_MIN;
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      if (c + u < c1) {
+        kpre[c + u] = run;
+        run = max(run, x[u]);
+      }
+  }
+}
+
+// per tile: every key's entry at pos_k, and the empty slots between pos_{k-1} and pos_k
+__global__ void __launch_bounds__(256) dir_place_kernel(const int32_t* __restrict__ rval, uint64_t n,
+                                                        const uint32_t* __restrict__ tile_off,
+                                                        const uint32_t* __restrict__ starts,
+                                                        const long long* __restrict__ kpre, DirHeader* hdr,
+                                                        uint4* __restrict__ dir) {
+  __shared__ uint32_t tmp[256 / 32 + 1];
+  __shared__ long long tmpl[256 / 32];
+  const uint64_t i0 = (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS;
+  DirRows r;
+  dir_rows(rval, n, i0, r);
+  uint32_t total;
+  uint64_t k = tile_off[blockIdx.x] + ej_block_exclusive_sum<256, uint32_t>((uint32_t)__popc(r.f), tmp, &total);
+  const unsigned long long nk = hdr->nkeys;
+  const uint32_t shift = 32u - hdr->bits;
+  long long m = LLONG_MIN;
+  uint64_t kk = k;
+#pragma unroll
+  for (int e = 0; e < DIR_ROWS; e++)
+    if (r.f >> e & 1u) {
+      m = max(m, (long long)(ej_hash32((uint32_t)r.v[e]) >> shift) - (long long)kk);
+      kk++;
+    }
+  long long all;
+  long long run = max(kpre[blockIdx.x], dir_block_exclusive_max(m, tmpl, &all));  // max over keys before k
+  long long prev = k ? (long long)k - 1 + run : -1;                                // pos_{k-1}
+#pragma unroll
+  for (int e = 0; e < DIR_ROWS; e++) {
+    if (!(r.f >> e & 1u)) continue;
+    const uint32_t hv = ej_hash32((uint32_t)r.v[e]);
+    run = max(run, (long long)(hv >> shift) - (long long)k);
+    const long long pos = (long long)k + run;
+    for (long long g = prev + 1; g < pos; g++) dir[g] = make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t s0 = (uint32_t)(i0 + e);
+    dir[pos] = make_uint4(hv, s0, starts[k + 1] - s0, 0u);
+    if (k == 0) hdr->pos_first = (unsigned long long)pos;
+    if (k + 1 == nk) hdr->pos_last = (unsigned long long)pos;
+    prev = pos;
+    k++;
+  }
+}
+
+// empty slots before the first entry and from one past the last to 2^bits
+// (all 2^bits + 1 slots when there are no keys)
+__global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restrict__ hdr, uint4* __restrict__ dir) {
+  const unsigned long long home_end = 1ull << hdr->bits;
+  const bool any = hdr->nkeys != 0;
+  const unsigned long long first = any ? hdr->pos_first : 0ull;
+  const unsigned long long tail = any ? hdr->pos_last + 1 : 0ull;
+  const unsigned long long tail_end = max(home_end, tail) + 1;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < first; i += stride)
+    dir[i] = make_uint4(0u, 0u, 0u, 0u);
+  for (uint64_t i = tail + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tail_end; i += stride)
+    dir[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // fence[i] = rval[i * EJ_FENCE_STRIDE] of a val-sorted table
@@ -103,8 +310,16 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta) {
 
 // ---- table build --------------------------------------------------------
 
+// directory slots reserved for nR rows: 2^bits <= next power of two of 2 nR,
+// plus one slot per key for the walk past the last home slot, plus the empty one
+static uint64_t ej_dir_capacity(uint64_t nR) {
+  uint64_t p = 2;
+  while (p < 2 * nR) p <<= 1;
+  return p + nR + 2;
+}
+
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
-  return tp.kind == EJ_TABLE_HASH ? (size_t(1) << tp.hb) * sizeof(uint2)
+  return tp.kind == EJ_TABLE_HASH ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint4)
                                   : (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
 }
 
@@ -125,6 +340,14 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
   tp.tmp_a_off = p.add(tuples);
   tp.tmp_b_off = p.add(tuples);
   ej_radix_plan_add(p, tp.rplan, nR);
+  if (kind == EJ_TABLE_HASH) {  // directory build scratch (the key starts reuse tmp_a)
+    const uint64_t tiles = (nR + DIR_TILE - 1) / DIR_TILE + 1;
+    tp.dir_keys_off = p.add(tiles * sizeof(uint32_t));
+    tp.dir_off_off = p.add((tiles + 1) * sizeof(uint32_t));
+    tp.dir_scan_off = p.add(ej_scan_scratch_bytes(tiles));
+    tp.dir_kmax_off = p.add(tiles * sizeof(long long));
+    tp.dir_kpre_off = p.add(tiles * sizeof(long long));
+  }
 }
 
 size_t ej_table_bytes(uint64_t nR, int delta) {
@@ -159,11 +382,32 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
   view->nR = tp.nR;
   view->hb = tp.hb;
   if (tp.kind == EJ_TABLE_HASH) {
-    uint2* bucket = static_cast<uint2*>(aux);
-    const uint64_t blocks = (tp.nR + 1 + 2047) / 2048;  // 256 rows per warp, 8 warps per block
-    bucket_start_kernel<<<(unsigned)blocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb);
-    EJ_TRY(ej_check_launch(h, "bucket_start_kernel"));
-    view->bucket = bucket;
+    DirHeader* hdr = static_cast<DirHeader*>(aux);
+    uint4* dir = reinterpret_cast<uint4*>(static_cast<char*>(aux) + DIR_HEADER_BYTES);
+    const uint32_t tiles = (uint32_t)((tp.nR + DIR_TILE - 1) / DIR_TILE);
+    uint32_t* starts = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.tmp_a_off));
+    uint32_t* keys = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.dir_keys_off));
+    uint32_t* off = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.dir_off_off));
+    long long* kmax = reinterpret_cast<long long*>(ej_arena_at(h, tp.dir_kmax_off));
+    long long* kpre = reinterpret_cast<long long*>(ej_arena_at(h, tp.dir_kpre_off));
+    if (tiles) {
+      dir_count_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, keys);
+      EJ_TRY(ej_check_launch(h, "dir_count_kernel"));
+      EJ_TRY(ej_scan_u32_u32(h, keys, tiles, off, ej_arena_at(h, tp.dir_scan_off)));
+      dir_compact_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, tiles, starts, kmax, hdr);
+      EJ_TRY(ej_check_launch(h, "dir_compact_kernel"));
+      dir_prefix_kernel<<<1, 1024, 0, h->stream>>>(kmax, tiles, kpre);
+      EJ_TRY(ej_check_launch(h, "dir_prefix_kernel"));
+      dir_place_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, starts, kpre, hdr, dir);
+      EJ_TRY(ej_check_launch(h, "dir_place_kernel"));
+    } else {  // no rows: no keys, two home slots
+      const DirHeader empty = {1u, 0u, 0ull, 0ull, 0ull};
+      EJ_CUDA(h, cudaMemcpyAsync(hdr, &empty, sizeof empty, cudaMemcpyHostToDevice, h->stream));
+    }
+    dir_edge_kernel<<<(unsigned)h->num_sms * 4, 256, 0, h->stream>>>(hdr, dir);
+    EJ_TRY(ej_check_launch(h, "dir_edge_kernel"));
+    view->dir = dir;
+    view->dir_bits = &hdr->bits;
   } else {
     int32_t* fence = static_cast<int32_t*>(aux);
     if (tp.nfence) {

@@ -15,6 +15,8 @@ struct ej_table_plan_t {
   uint32_t nfence = 0;  // sorted index: fence entries
   // arena offsets; rkey/rval/aux are unused when the table has its own storage
   size_t rkey_off = 0, rval_off = 0, aux_off = 0, tmp_a_off = 0, tmp_b_off = 0;
+  // key directory build scratch (hash tables)
+  size_t dir_keys_off = 0, dir_off_off = 0, dir_scan_off = 0, dir_kmax_off = 0, dir_kpre_off = 0;
   ej_radix_plan rplan;
 };
 

@@ -2,10 +2,13 @@
 //
 // A table stores R as rkey[]/rval[] in one order (ej_table_view).  In both
 // kinds the matches of a value v form one contiguous run [lo, lo + c):
-//   EJ_TABLE_HASH    rows sorted by hash32(val); the run lies inside bucket
-//                    b = top hb hash bits, rows [bucket[b].x, bucket[b].y)
-//                    (one 8-byte load), found by scanning the bucket with
-//                    16-byte vector loads of rval;
+//   EJ_TABLE_HASH    rows sorted by hash32(val).  Single tables carry a key
+//                    directory (one 16-byte entry {hash, lo, c} per distinct
+//                    key, in hash order, linear probing from slot hash >>
+//                    (32 - bits)); batched tables carry bucket bounds: the run
+//                    lies inside bucket b = top hb hash bits, rows
+//                    [bucket[b].x, bucket[b].y) (one 8-byte load), found by
+//                    scanning the bucket with 16-byte vector loads of rval;
 //   EJ_TABLE_SORTED  rows sorted by val; lower and upper bounds by binary
 //                    search, first over the fence (every 256th val), then
 //                    inside one 256-row segment.
@@ -71,6 +74,28 @@ struct EjRun;
 template <int N>
 __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const int32_t (&v)[N], const bool (&ok)[N],
                                                   uint32_t (&lo)[N], uint32_t (&c)[N]) {
+  if (t.dir) {
+    // key directory: one 16-byte entry {hash, start, length, 0} answers most
+    // probes; the walk goes on past smaller hashes (entries are in hash order)
+    // and stops at the probe's hash, a larger one or an empty slot
+    const uint32_t shift = 32u - __ldg(t.dir_bits);
+    uint32_t hv[N], slot[N];
+    uint4 e[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      hv[j] = ej_hash32((uint32_t)v[j]);
+      slot[j] = hv[j] >> shift;
+      e[j] = ok[j] ? __ldg(t.dir + slot[j]) : make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      while (e[j].z != 0u && e[j].x < hv[j]) e[j] = __ldg(t.dir + ++slot[j]);
+      const bool hit = e[j].z != 0u && e[j].x == hv[j];
+      lo[j] = hit ? e[j].y : 0u;
+      c[j] = hit ? e[j].z : 0u;
+    }
+    return;
+  }
   uint32_t s0[N], s1[N];
 #pragma unroll
   for (int j = 0; j < N; j++) {
