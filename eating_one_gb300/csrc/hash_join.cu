@@ -262,12 +262,21 @@ __global__ void fence_kernel(const int32_t* __restrict__ rval, int32_t* __restri
 // ---- count, then write from the run descriptors ---------------------------------
 // (probe_write.cuh); the warp-tile totals are scanned in between
 
+// L2 prefetch of the 1 KB of one warp tile's probe tuples (or descriptors,
+// also 8 bytes per probe), one 128-byte line per lane of the first eight;
+// lines past the nP probes are skipped
+__device__ __forceinline__ void ej_prefetch_tile(const void* base, uint64_t w, uint64_t nP, unsigned lane) {
+  const uint64_t off = w * (PR_WTILE * 8) + (uint64_t)lane * 128u;
+  if (lane < 8u && off < nP * 8) asm volatile("prefetch.global.L2 [%0];" ::"l"(static_cast<const char*>(base) + off));
+}
+
 template <int KIND, bool OUTER, bool DESC>
 __global__ void __launch_bounds__(PR_THREADS, 5)  // 40 warps per SM hide the table loads
 probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* __restrict__ wcount,
-                   uint64_t nwtiles, uint2* __restrict__ desc) {
+                   uint64_t nwtiles, uint2* __restrict__ desc, uint64_t ahead) {
   const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + (threadIdx.x >> 5);
   if (w >= nwtiles) return;
+  ej_prefetch_tile(P, w + ahead, nP, threadIdx.x & 31u);  // the tile a warp one resident wave later takes
   const unsigned long long total = ej_probe_count_warp_desc<KIND, OUTER, DESC>(P, w * PR_WTILE, nP, t, desc);
   if ((threadIdx.x & 31u) == 0) wcount[w] = total;
 }
@@ -275,12 +284,14 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
 __global__ void __launch_bounds__(PR_THREADS)
 probe_write_kernel(const ej_tuple* __restrict__ P, const uint2* __restrict__ desc, uint64_t nP, ej_table_view t,
                    const unsigned long long* __restrict__ woff, uint64_t nwtiles, ej_result* __restrict__ out,
-                   uint64_t cap, ej_dev_status* st) {
+                   uint64_t cap, ej_dev_status* st, uint64_t ahead) {
   __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
   const unsigned int warp = threadIdx.x >> 5;
   const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + warp;
   if (w >= nwtiles) return;
   if (w == 0 && threadIdx.x == 0 && woff[nwtiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  ej_prefetch_tile(P, w + ahead, nP, threadIdx.x & 31u);  // the tile a warp one resident wave later takes
+  ej_prefetch_tile(desc, w + ahead, nP, (threadIdx.x & 31u) - 8u);
   const unsigned long long off = woff[w];
   if (off >= cap) return;
   ej_probe_write_warp(P, desc, w * PR_WTILE, nP, t, off, out, cap, stage[warp]);
@@ -291,10 +302,12 @@ ej_status launch_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* 
                        unsigned long long* wcount, uint2* desc) {
   if (desc)
     probe_count_kernel<KIND, OUTER, true>
-        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, desc);
+        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, desc,
+                                                            (uint64_t)h->num_sms * 5 * PR_WARPS);
   else
     probe_count_kernel<KIND, OUTER, false>
-        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, nullptr);
+        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, nullptr,
+                                                            (uint64_t)h->num_sms * 5 * PR_WARPS);
   return ej_check_launch(h, "probe_count_kernel");
 }
 
@@ -463,7 +476,8 @@ ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
   const uint2* desc = reinterpret_cast<const uint2*>(ej_arena_at(h, pp.desc_off));
   const unsigned long long* woff = reinterpret_cast<const unsigned long long*>(ej_arena_at(h, pp.off_off));
   probe_write_kernel<<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, desc, pp.nP, t, woff, pp.nwtiles, out,
-                                                                        cap, h->d_status);
+                                                                        cap, h->d_status,
+                                                                        (uint64_t)h->num_sms * 4 * PR_WARPS);
   return ej_check_launch(h, "probe_write_kernel");
 }
 
