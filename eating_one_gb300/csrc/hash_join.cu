@@ -491,9 +491,10 @@ uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS) {
   const double table = (double)ej_table_bytes(nR, ej_tuned_bucket_delta(h, nR));
   const double l2 = (double)(h->l2_bytes ? h->l2_bytes : (size_t)126 << 20);
   if (table <= l2 / 4.0) return 0;  // the whole table stays L2-resident
-  // one partition's table region should be a few MB so that the partitions in
-  // flight (about two) share L2 with the streaming probe and output traffic
-  uint32_t pb = ej_ceil_log2((uint64_t)(table / (l2 / 32.0)) + 1);
+  // one partition's table region should be several MB so that the partitions
+  // in flight share L2 with the streaming probe and output traffic (C3's
+  // 2^26-row tables: 7 bits; 5 to 8 bits measured within 2 % of each other)
+  uint32_t pb = ej_ceil_log2((uint64_t)(table / (l2 / 16.0)) + 1);
   if (pb > 8) pb = 8;
   if (pb > hb) pb = hb;
   return pb;
