@@ -297,6 +297,41 @@ probe_write_kernel(const ej_tuple* __restrict__ P, const uint2* __restrict__ des
   ej_probe_write_warp(P, desc, w * PR_WTILE, nP, t, off, out, cap, stage[warp]);
 }
 
+// One pass (the joins that materialise rows in one call): each warp finds the
+// runs of its 128 probes, reserves its rows with one atomic add on the row
+// cursor, and writes them through its staging buffer as the write pass does.
+// Warps take their row ranges in the order they reach the cursor, so the row
+// order is not deterministic (the multiset is); rows at or past cap are
+// dropped, the cursor ends at the exact count.
+template <int KIND, bool OUTER>
+__global__ void __launch_bounds__(PR_THREADS)
+probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, uint64_t nwtiles,
+                   unsigned long long* __restrict__ cursor, ej_result* __restrict__ out, uint64_t cap,
+                   ej_dev_status* st, uint64_t ahead) {
+  __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
+  const unsigned int warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + warp;
+  if (w >= nwtiles) return;
+  ej_prefetch_tile(P, w + ahead, nP, lane);  // the tile a warp one resident wave later takes
+  EjProbeWarp pw;
+  ej_probe_runs_warp<KIND, OUTER>(P, w * PR_WTILE, nP, t, pw);
+  unsigned long long mine = 0;
+#pragma unroll
+  for (int j = 0; j < PR_ITEMS; j++) mine += pw.cnt[j];
+  const unsigned long long total = ej_warp_sum<unsigned long long>(mine);
+  if (total == 0) return;
+  unsigned long long off = 0;
+  if (lane == 0) {
+    off = atomicAdd(cursor, total);
+    if (off + total > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  }
+  off = __shfl_sync(EJ_FULL_MASK, off, 0);
+  if (off >= cap) return;
+  int32_t kk[PR_ITEMS][PW_PREFETCH];
+  ej_probe_prefetch(t, pw, kk);
+  ej_emit_warp(pw, kk, t, off, out, cap, stage[warp]);
+}
+
 template <int KIND, bool OUTER>
 ej_status launch_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                        unsigned long long* wcount, uint2* desc) {
@@ -502,13 +537,34 @@ uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS) {
 
 // ---- probe drivers -------------------------------------------------------
 
-void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only) {
+void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only,
+                         bool two_pass) {
   L.pb = pb;
   if (pb) {
     L.spart_off = p.add((size_t)nS * sizeof(ej_tuple));
     ej_radix_plan_add(p, L.splan, nS);
   }
-  ej_probe_plan(p, L.pp, nS, !count_only);
+  ej_probe_plan(p, L.pp, nS, !count_only && two_pass);
+}
+
+template <int KIND, bool OUTER>
+static ej_status launch_fused(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
+                              unsigned long long* cursor, ej_result* out, uint64_t cap) {
+  probe_fused_kernel<KIND, OUTER><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(
+      P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 4 * PR_WARPS);
+  return ej_check_launch(h, "probe_fused_kernel");
+}
+
+// [partition +] the fused pass; the count ends in *cursor (zeroed here)
+static ej_status ej_probe_fused(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
+                                bool outer, ej_result* out, uint64_t cap, unsigned long long* cursor) {
+  EJ_CUDA(h, cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), h->stream));
+  if (!pp.ntiles) return EJ_OK;
+  if (t.kind == EJ_TABLE_HASH)
+    return outer ? launch_fused<EJ_TABLE_HASH, true>(h, pp, P, t, cursor, out, cap)
+                 : launch_fused<EJ_TABLE_HASH, false>(h, pp, P, t, cursor, out, cap);
+  return outer ? launch_fused<EJ_TABLE_SORTED, true>(h, pp, P, t, cursor, out, cap)
+               : launch_fused<EJ_TABLE_SORTED, false>(h, pp, P, t, cursor, out, cap);
 }
 
 // Partition S (when the layout says so), count (+ scan), then write unless
@@ -526,9 +582,14 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
     P = spart;
   }
   ej_phase_mark(h, 2);
-  EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
-  ej_phase_mark(h, 3);
-  if (!count_only) EJ_TRY(ej_probe_write(h, L.pp, P, t, out, out_cap));
+  if (count_only || L.pp.with_desc) {  // the count pass, then (planned two-pass) rows in probe order
+    EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
+    ej_phase_mark(h, 3);
+    if (!count_only) EJ_TRY(ej_probe_write(h, L.pp, P, t, out, out_cap));
+  } else {
+    ej_phase_mark(h, 3);  // one pass: recorded as the write phase
+    EJ_TRY(ej_probe_fused(h, L.pp, P, t, outer, out, out_cap, d_count ? d_count : h->d_words + 3));
+  }
   ej_phase_mark(h, 4);
   return EJ_OK;
 }
@@ -541,7 +602,9 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   ej_table_plan_t tp;
   ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR));
   ej_probe_layout L;
-  ej_probe_layout_add(p, L, nS, pb, mode == 2);
+  // the build-side-only join keeps its rows in probe order (the batched joins
+  // give the same rows in the same order); the others take the one-pass probe
+  ej_probe_layout_add(p, L, nS, pb, mode == 2, /*two_pass=*/mode == 1);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t;

@@ -57,7 +57,10 @@ ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
                          ej_result* out, uint64_t cap);
 
 uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS);
-void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only);
+// two_pass: plan the run descriptors of ej_probe_count + ej_probe_write (for
+// callers that read the count in between); ej_probe_exec needs none
+void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only,
+                         bool two_pass = false);
 ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_view& t, const ej_tuple* S,
                         bool outer, bool count_only, ej_result* out, uint64_t out_cap,
                         unsigned long long* d_count);

@@ -215,7 +215,7 @@ struct HashChunk {
 ej_status sj_hash_begin(ej_handle* h, ej_stream_res* r, Job& j, const ej_tuple* Sd, uint64_t n, HashChunk& c) {
   ej_plan_bytes p;
   p.bytes = j.probe_base;
-  ej_probe_layout_add(p, c.L, n, j.pb, false);  // within the space reserved for a full chunk
+  ej_probe_layout_add(p, c.L, n, j.pb, false, true);  // within the space reserved for a full chunk
   if (p.bytes > h->arena_cap) return ej_fail(h, EJ_ERR_INTERNAL, "chunk probe layout exceeds its reservation");
   c.P = Sd;
   if (c.L.pb) {
@@ -352,7 +352,7 @@ extern "C" ej_status ej_join_host_chunked(ej_handle* h, ej_algo algo, const ej_t
       j.probe_base = p.bytes;
       j.pb = ej_probe_partition_bits(h, nb, s_chunk);
       ej_probe_layout L;
-      ej_probe_layout_add(p, L, s_chunk, j.pb, false);
+      ej_probe_layout_add(p, L, s_chunk, j.pb, false, true);
       EJ_TRY(ej_arena_reserve(h, p.bytes));
       EJ_TRY(ej_table_build(h, tp, dR, reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rkey_off)),
                             reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rval_off)), ej_arena_at(h, tp.aux_off),

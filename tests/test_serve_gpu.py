@@ -38,7 +38,11 @@ def test_results_same_alone_and_in_mix(engine, pool, mode):
     for c in comps:
         assert c.status == native.EJ_OK
         assert c.count == pool.expected[c.tag] == alone[c.tag].shape[0]
-        assert torch.equal(pool.out[c.tag][: c.count], alone[c.tag])
+        got = pool.out[c.tag][: c.count]
+        if mode == BATCHED:  # the batched pipeline keeps the build-side-only join's row order
+            assert torch.equal(got, alone[c.tag])
+        else:  # one hash join per request: the same rows, order unspecified
+            assert np.array_equal(O.canon(got.cpu().numpy()), O.canon(alone[c.tag].cpu().numpy()))
     if mode == BATCHED:
         assert max(c.batch_joins for c in comps) > 1
     for i in (0, 5, 17):
