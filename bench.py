@@ -4,8 +4,8 @@
 One step = the three hash joins of configuration C3 (R = 2^26 tuples holding
 2^24 distinct keys x4, S = 2^28 tuples with Zipf(s) keys over R's keys, 10% of
 S from an absent key range, s in {0, 0.75, 1}), each run end to end on the
-device: R table build (LSD radix passes + bucket starts), one S radix pass,
-count pass, look-back scan, write pass of every result row.  Inputs are
+device: R table build (LSD radix passes + key directory), one S radix pass,
+one probe pass that finds, reserves and writes every result row.  Inputs are
 generated on the device with seeded integer generators (synthetic data;
 every input is far larger than the 126 MB L2).
 
@@ -593,10 +593,10 @@ def main() -> None:
     n_s = sum(j["S"].shape[0] for j in joins) / len(joins)
     n_r = sum(j["R"].shape[0] for j in joins) / len(joins)
     n_o = sum(j["n_out"] for j in joins) / len(joins)
-    names = ["build (R table: LSD radix passes + bucket starts)", "partition (S radix pass)",
-             "count (probe_count_kernel + scan)", "write (probe_write_kernel)"]
+    names = ["build (R table: LSD radix passes + key directory)", "partition (S radix pass)",
+             "count (none: the probe is one pass)", "probe (probe_fused_kernel: find, reserve, write)"]
     kernel = ["rx_scatter_kernel+rx_hist_kernel (R)", "rx_scatter_kernel+rx_hist_kernel (S)",
-              "probe_count_kernel", "probe_write_kernel"]
+              "probe_count_kernel", "probe_fused_kernel"]
     # algorithmic bytes per launch of each phase
     phase_bytes = [24.0 * n_r * 3 + 4.0 * n_r, 24.0 * n_s, 8.0 * n_s, 8.0 * n_s + 16.0 * n_o]
     per_join = [p / max(njoins, 1) for p in phases]

@@ -320,6 +320,10 @@ probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   for (int j = 0; j < PR_ITEMS; j++) mine += pw.cnt[j];
   const unsigned long long total = ej_warp_sum<unsigned long long>(mine);
   if (total == 0) return;
+  // the run keys and the row reservation travel together: the key loads are
+  // issued first and do not wait for the atomic's answer
+  int32_t kk[PR_ITEMS][PW_PREFETCH];
+  ej_probe_prefetch(t, pw, kk);
   unsigned long long off = 0;
   if (lane == 0) {
     off = atomicAdd(cursor, total);
@@ -327,8 +331,6 @@ probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   }
   off = __shfl_sync(EJ_FULL_MASK, off, 0);
   if (off >= cap) return;
-  int32_t kk[PR_ITEMS][PW_PREFETCH];
-  ej_probe_prefetch(t, pw, kk);
   ej_emit_warp(pw, kk, t, off, out, cap, stage[warp]);
 }
 
