@@ -168,7 +168,7 @@ struct ej_table_view {
   const int32_t* rkey = nullptr;     // [nR + pad] row ids in table order
   const int32_t* rval = nullptr;     // [nR + pad] join keys in table order
   const uint2* bucket = nullptr;     // [2^hb] (hash, batched tables): row bounds of each bucket
-  const uint4* dir = nullptr;        // (hash, single tables) key directory {hash, start, length, 0}
+  const uint2* dir = nullptr;        // (hash, single tables) key directory {hash, run start}
   const uint32_t* dir_bits = nullptr;  // device word: the directory has 2^bits home slots
   const int32_t* fence = nullptr;    // [nfence] (sorted)
   uint64_t nR = 0;

@@ -41,25 +41,27 @@ namespace {
 
 // ---- key directory of a hash table ----------------------------------------
 // The distinct keys of the hash-sorted table, in hash order, each an entry
-// {hash, run start, run length, 0} placed by linear probing from its home slot
+// {hash, run start} placed by linear probing from its home slot
 // hash >> (32 - bits), 2^bits >= 2 x keys: key k goes to
 //   pos_k = max(home_k, pos_{k-1} + 1) = k + max_{j <= k} (home_j - j),
-// so the entries stay in hash order and a probe walks forward from its home
-// slot past smaller hashes until it meets its hash, a larger one or an empty
-// slot (length 0).  Each key also writes the empty slots between its
-// predecessor's entry and its own; dir_edge_kernel empties the slots before
-// the first entry and after the last (up to 2^bits, and one past the last
-// entry).  The number of keys, and so bits, is known only on the device: it
-// lives in the header in front of the entries.  Build: per 4096-row tile,
-// count the rows that begin a key; scan; per tile, the key starts and the
-// largest home_k - k; a prefix maximum over the tiles; per tile, the entries.
+// so the entries stay in hash order.  Every slot holds the first key at or
+// after it: the slots between pos_{k-1} and pos_k hold copies of key k, the
+// slots past the last entry a sentinel {0xFFFFFFFF, nR}.  A probe walks
+// forward from its home slot past smaller hashes; it has found its key when
+// the hash matches and the start is below nR, and the run ends at the first
+// later slot whose start differs (the next key's start).  The number of keys,
+// and so bits, is known only on the device: it lives in the header in front
+// of the entries.  Build: per 4096-row tile, count the rows that begin a key;
+// scan; per tile, the largest home_k - k; a prefix maximum over the tiles;
+// per tile, every key's slots (pos_{k-1}, pos_k]; then the slots before the
+// first entry and after the last.
 
 constexpr int DIR_ROWS = 16;              // consecutive rows per thread
 constexpr int DIR_TILE = 256 * DIR_ROWS;  // rows per block
 
 struct DirHeader {
   uint32_t bits;
-  uint32_t pad;
+  uint32_t hash0;  // hash of the first key
   unsigned long long nkeys;
   unsigned long long pos_first, pos_last;  // slots of the first and last entries
 };
@@ -134,12 +136,10 @@ __global__ void __launch_bounds__(256) dir_count_kernel(const int32_t* __restric
   if (threadIdx.x == 0) tile_keys[blockIdx.x] = total;
 }
 
-// per tile: the start row of each of its keys (starts[nkeys] = n) and the
-// largest home_k - k; the header's key count and bits
-__global__ void __launch_bounds__(256) dir_compact_kernel(const int32_t* __restrict__ rval, uint64_t n,
+// per tile: the largest home_k - k; the header (key count, bits, first hash)
+__global__ void __launch_bounds__(256) dir_tilemax_kernel(const int32_t* __restrict__ rval, uint64_t n,
                                                           const uint32_t* __restrict__ tile_off, uint32_t ntiles,
-                                                          uint32_t* __restrict__ starts, long long* __restrict__ kmax,
-                                                          DirHeader* hdr) {
+                                                          long long* __restrict__ kmax, DirHeader* hdr) {
   __shared__ uint32_t tmp[256 / 32 + 1];
   __shared__ long long tmpl[256 / 32];
   const uint64_t i0 = (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS;
@@ -148,12 +148,11 @@ __global__ void __launch_bounds__(256) dir_compact_kernel(const int32_t* __restr
   uint32_t total;
   uint64_t k = tile_off[blockIdx.x] + ej_block_exclusive_sum<256, uint32_t>((uint32_t)__popc(r.f), tmp, &total);
   const unsigned long long nk = tile_off[ntiles];
-  const uint32_t shift = 32u - dir_bits_for(nk);
+  const uint32_t bits = dir_bits_for(nk), shift = 32u - bits;
   long long m = LLONG_MIN;
 #pragma unroll
   for (int e = 0; e < DIR_ROWS; e++)
     if (r.f >> e & 1u) {
-      starts[k] = (uint32_t)(i0 + e);
       m = max(m, (long long)(ej_hash32((uint32_t)r.v[e]) >> shift) - (long long)k);
       k++;
     }
@@ -161,8 +160,8 @@ __global__ void __launch_bounds__(256) dir_compact_kernel(const int32_t* __restr
   dir_block_exclusive_max(m, tmpl, &all);
   if (threadIdx.x == 0) kmax[blockIdx.x] = all;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    starts[nk] = (uint32_t)n;
-    hdr->bits = 32u - shift;
+    hdr->bits = bits;
+    hdr->hash0 = ej_hash32((uint32_t)r.v[0]);  // row 0 begins the first key
     hdr->nkeys = nk;
   }
 }
@@ -196,12 +195,11 @@ __global__ void __launch_bounds__(1024) dir_prefix_kernel(const long long* __res
   }
 }
 
-// per tile: every key's entry at pos_k, and the empty slots between pos_{k-1} and pos_k
+// per tile: every key's slots (pos_{k-1}, pos_k], holding {hash_k, start_k}
 __global__ void __launch_bounds__(256) dir_place_kernel(const int32_t* __restrict__ rval, uint64_t n,
                                                         const uint32_t* __restrict__ tile_off,
-                                                        const uint32_t* __restrict__ starts,
                                                         const long long* __restrict__ kpre, DirHeader* hdr,
-                                                        uint4* __restrict__ dir) {
+                                                        uint2* __restrict__ dir) {
   __shared__ uint32_t tmp[256 / 32 + 1];
   __shared__ long long tmpl[256 / 32];
   const uint64_t i0 = (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS;
@@ -228,9 +226,9 @@ __global__ void __launch_bounds__(256) dir_place_kernel(const int32_t* __restric
     const uint32_t hv = ej_hash32((uint32_t)r.v[e]);
     run = max(run, (long long)(hv >> shift) - (long long)k);
     const long long pos = (long long)k + run;
-    for (long long g = prev + 1; g < pos; g++) dir[g] = make_uint4(0u, 0u, 0u, 0u);
-    const uint32_t s0 = (uint32_t)(i0 + e);
-    dir[pos] = make_uint4(hv, s0, starts[k + 1] - s0, 0u);
+    const uint2 entry = make_uint2(hv, (uint32_t)(i0 + e));
+    // key 0's leading slots [0, pos_0) are written by dir_edge_kernel
+    for (long long g = (k ? prev + 1 : pos); g <= pos; g++) dir[g] = entry;
     if (k == 0) hdr->pos_first = (unsigned long long)pos;
     if (k + 1 == nk) hdr->pos_last = (unsigned long long)pos;
     prev = pos;
@@ -238,19 +236,22 @@ __global__ void __launch_bounds__(256) dir_place_kernel(const int32_t* __restric
   }
 }
 
-// empty slots before the first entry and from one past the last to 2^bits
-// (all 2^bits + 1 slots when there are no keys)
-__global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restrict__ hdr, uint4* __restrict__ dir) {
+// the slots before the first entry (copies of the first key) and from one
+// past the last entry to 2^bits + 1, at least two of them (sentinels
+// {0xFFFFFFFF, n}; a probe reads the slot after the one it stops at); with no
+// keys, slots [0, 2^bits + 1]
+__global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restrict__ hdr, uint64_t n,
+                                                       uint2* __restrict__ dir) {
   const unsigned long long home_end = 1ull << hdr->bits;
   const bool any = hdr->nkeys != 0;
   const unsigned long long first = any ? hdr->pos_first : 0ull;
   const unsigned long long tail = any ? hdr->pos_last + 1 : 0ull;
-  const unsigned long long tail_end = max(home_end, tail) + 1;
+  const unsigned long long tail_end = max(home_end, tail) + 2;
+  const uint2 lead = make_uint2(hdr->hash0, 0u), sentinel = make_uint2(0xFFFFFFFFu, (uint32_t)n);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < first; i += stride)
-    dir[i] = make_uint4(0u, 0u, 0u, 0u);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < first; i += stride) dir[i] = lead;
   for (uint64_t i = tail + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tail_end; i += stride)
-    dir[i] = make_uint4(0u, 0u, 0u, 0u);
+    dir[i] = sentinel;
 }
 
 // fence[i] = rval[i * EJ_FENCE_STRIDE] of a val-sorted table
@@ -361,7 +362,8 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta) {
 // ---- table build --------------------------------------------------------
 
 // directory slots reserved for nR rows: 2^bits <= next power of two of 2 nR,
-// plus one slot per key for the walk past the last home slot, plus the empty one
+// plus one slot per key for the entries past the last home slot, plus two
+// sentinels (the last written slot is at most 2^bits + keys)
 static uint64_t ej_dir_capacity(uint64_t nR) {
   uint64_t p = 2;
   while (p < 2 * nR) p <<= 1;
@@ -369,7 +371,7 @@ static uint64_t ej_dir_capacity(uint64_t nR) {
 }
 
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
-  return tp.kind == EJ_TABLE_HASH ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint4)
+  return tp.kind == EJ_TABLE_HASH ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint2)
                                   : (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
 }
 
@@ -390,7 +392,7 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
   tp.tmp_a_off = p.add(tuples);
   tp.tmp_b_off = p.add(tuples);
   ej_radix_plan_add(p, tp.rplan, nR);
-  if (kind == EJ_TABLE_HASH) {  // directory build scratch (the key starts reuse tmp_a)
+  if (kind == EJ_TABLE_HASH) {  // directory build scratch
     const uint64_t tiles = (nR + DIR_TILE - 1) / DIR_TILE + 1;
     tp.dir_keys_off = p.add(tiles * sizeof(uint32_t));
     tp.dir_off_off = p.add((tiles + 1) * sizeof(uint32_t));
@@ -433,9 +435,8 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
   view->hb = tp.hb;
   if (tp.kind == EJ_TABLE_HASH) {
     DirHeader* hdr = static_cast<DirHeader*>(aux);
-    uint4* dir = reinterpret_cast<uint4*>(static_cast<char*>(aux) + DIR_HEADER_BYTES);
+    uint2* dir = reinterpret_cast<uint2*>(static_cast<char*>(aux) + DIR_HEADER_BYTES);
     const uint32_t tiles = (uint32_t)((tp.nR + DIR_TILE - 1) / DIR_TILE);
-    uint32_t* starts = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.tmp_a_off));
     uint32_t* keys = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.dir_keys_off));
     uint32_t* off = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.dir_off_off));
     long long* kmax = reinterpret_cast<long long*>(ej_arena_at(h, tp.dir_kmax_off));
@@ -444,17 +445,17 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
       dir_count_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, keys);
       EJ_TRY(ej_check_launch(h, "dir_count_kernel"));
       EJ_TRY(ej_scan_u32_u32(h, keys, tiles, off, ej_arena_at(h, tp.dir_scan_off)));
-      dir_compact_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, tiles, starts, kmax, hdr);
-      EJ_TRY(ej_check_launch(h, "dir_compact_kernel"));
+      dir_tilemax_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, tiles, kmax, hdr);
+      EJ_TRY(ej_check_launch(h, "dir_tilemax_kernel"));
       dir_prefix_kernel<<<1, 1024, 0, h->stream>>>(kmax, tiles, kpre);
       EJ_TRY(ej_check_launch(h, "dir_prefix_kernel"));
-      dir_place_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, starts, kpre, hdr, dir);
+      dir_place_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, kpre, hdr, dir);
       EJ_TRY(ej_check_launch(h, "dir_place_kernel"));
     } else {  // no rows: no keys, two home slots
       const DirHeader empty = {1u, 0u, 0ull, 0ull, 0ull};
       EJ_CUDA(h, cudaMemcpyAsync(hdr, &empty, sizeof empty, cudaMemcpyHostToDevice, h->stream));
     }
-    dir_edge_kernel<<<(unsigned)h->num_sms * 4, 256, 0, h->stream>>>(hdr, dir);
+    dir_edge_kernel<<<(unsigned)h->num_sms * 4, 256, 0, h->stream>>>(hdr, tp.nR, dir);
     EJ_TRY(ej_check_launch(h, "dir_edge_kernel"));
     view->dir = dir;
     view->dir_bits = &hdr->bits;

@@ -3,9 +3,10 @@
 // A table stores R as rkey[]/rval[] in one order (ej_table_view).  In both
 // kinds the matches of a value v form one contiguous run [lo, lo + c):
 //   EJ_TABLE_HASH    rows sorted by hash32(val).  Single tables carry a key
-//                    directory (one 16-byte entry {hash, lo, c} per distinct
-//                    key, in hash order, linear probing from slot hash >>
-//                    (32 - bits)); batched tables carry bucket bounds: the run
+//                    directory (8-byte entries {hash, lo} in hash order,
+//                    linear probing from slot hash >> (32 - bits), each slot
+//                    holding the first key at or after it, so c is the next
+//                    slot's start minus lo); batched tables carry bucket bounds: the run
 //                    lies inside bucket b = top hb hash bits, rows
 //                    [bucket[b].x, bucket[b].y) (one 8-byte load), found by
 //                    scanning the bucket with 16-byte vector loads of rval;
@@ -75,24 +76,43 @@ template <int N>
 __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const int32_t (&v)[N], const bool (&ok)[N],
                                                   uint32_t (&lo)[N], uint32_t (&c)[N]) {
   if (t.dir) {
-    // key directory: one 16-byte entry {hash, start, length, 0} answers most
-    // probes; the walk goes on past smaller hashes (entries are in hash order)
-    // and stops at the probe's hash, a larger one or an empty slot
+    // key directory: every slot holds the first key at or after it; walk past
+    // smaller hashes, then the run ends at the first slot with another start
+    // (slot + 1 never passes the sentinels after the last entry)
     const uint32_t shift = 32u - __ldg(t.dir_bits);
     uint32_t hv[N], slot[N];
-    uint4 e[N];
+    uint2 a[N], b[N];
 #pragma unroll
     for (int j = 0; j < N; j++) {
       hv[j] = ej_hash32((uint32_t)v[j]);
       slot[j] = hv[j] >> shift;
-      e[j] = ok[j] ? __ldg(t.dir + slot[j]) : make_uint4(0u, 0u, 0u, 0u);
+      a[j] = b[j] = make_uint2(0u, 0u);
+      if (ok[j]) {
+        // the 16-byte aligned slot pair holding the home slot (the directory
+        // starts 16-byte aligned): both slots needed when it is even
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(t.dir) + (slot[j] >> 1));
+        if (slot[j] & 1u) {
+          a[j] = make_uint2(q.z, q.w);
+          b[j] = __ldg(t.dir + slot[j] + 1);
+        } else {
+          a[j] = make_uint2(q.x, q.y);
+          b[j] = make_uint2(q.z, q.w);
+        }
+      }
     }
 #pragma unroll
     for (int j = 0; j < N; j++) {
-      while (e[j].z != 0u && e[j].x < hv[j]) e[j] = __ldg(t.dir + ++slot[j]);
-      const bool hit = e[j].z != 0u && e[j].x == hv[j];
-      lo[j] = hit ? e[j].y : 0u;
-      c[j] = hit ? e[j].z : 0u;
+      lo[j] = 0u;
+      c[j] = 0u;
+      if (!ok[j]) continue;
+      while (a[j].x < hv[j]) {
+        a[j] = b[j];
+        b[j] = __ldg(t.dir + ++slot[j] + 1);
+      }
+      if (a[j].x != hv[j] || a[j].y >= t.nR) continue;
+      while (b[j].y == a[j].y) b[j] = __ldg(t.dir + ++slot[j] + 1);
+      lo[j] = a[j].y;
+      c[j] = b[j].y - a[j].y;
     }
     return;
   }
