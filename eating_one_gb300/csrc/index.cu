@@ -100,7 +100,9 @@ static ej_status index_probe(ej_handle* h, const ej_index* ix, const ej_tuple* S
   const uint32_t pb = ix->kind == EJ_TABLE_HASH ? ej_probe_partition_bits(h, ix->nR, nS) : 0u;
   ej_plan_bytes p;
   ej_probe_layout L;
-  ej_probe_layout_add(p, L, nS, pb, count_only);
+  // a sorted index's run search (two binary searches) is long: it runs once,
+  // in the count pass, and the write pass reads the run descriptors
+  ej_probe_layout_add(p, L, nS, pb, count_only, /*two_pass=*/ix->kind == EJ_TABLE_SORTED);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_phase_mark(h, 1);
