@@ -9,15 +9,14 @@
 //   build       four segmented LSD radix passes: tiles never cross a join and
 //               the digit histograms are laid out join by join, so one scan
 //               places every join's rows in its own range, hash-sorted
-//   starts      every join's bucket starts in one launch (its own bucket bits)
-//   count       one launch over every join's probe tiles: run descriptors and
-//               warp-tile row totals, joins laid out one after the other;
-//   scan        of all the warp-tile totals at once;
-//   write       one launch: a warp tile's offset within its join is the scan
-//               minus the scan at the join's first warp tile; the first warp
-//               tile of a join stores the join's count.
-// Every join's rows are bitwise the same as when it runs alone: the same
-// table order (stable passes over the same rows) and the same tile order.
+//   starts      every join's bucket starts in one launch (its own bucket bits;
+//               a batch's tables are small enough for L2, where the bucket
+//               scan is as fast as a key directory and one launch builds it)
+//   probe       one launch over every join's probe tiles: each warp finds its
+//               runs, reserves its rows with one atomic add on its join's
+//               count and writes them (the one-pass probe of single joins).
+// Every join's rows are the rows it gives alone; their order within the join
+// is not specified (warps reserve their ranges in the order they arrive).
 #include "ej_device.cuh"
 #include "ej_entry.h"
 #include "hash_join.cuh"
@@ -34,12 +33,10 @@ struct BatchJoin {
   const ej_tuple* S;
   ej_result* out;
   unsigned long long cap;
-  unsigned long long* d_count;
+  unsigned long long* d_count;  // the join's row cursor, then its count
   unsigned long long nS;
-  unsigned long long first_wtile;  // first warp tile of the join in the batch's warp-tile order
-  unsigned long long nwtiles;      // warp tiles of the join
-  unsigned long long desc0;        // first run descriptor of the join in the batch's array
-  unsigned long long r_row0;       // first row of the join in the concatenated R
+  unsigned long long nwtiles;  // warp tiles of the join
+  unsigned long long r_row0;   // first row of the join in the concatenated R
   const ej_tuple* R;
 };
 
@@ -75,40 +72,34 @@ __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, 
     ej_bucket_bounds_warp(t.rval, t.nR, r0, t.hb, bucket);
 }
 
-// count pass over every join's warp tiles (block = one 1024-probe tile of
-// one join), run descriptors into the batch's array
-__global__ void __launch_bounds__(PR_THREADS, 5)
-batch_count_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
-                   unsigned long long* __restrict__ wcount, uint2* __restrict__ desc) {
-  const BatchPTile pt = ptiles[blockIdx.x];
-  const BatchJoin& j = joins[pt.join];
-  const uint64_t w = (uint64_t)pt.local * PR_WARPS + (threadIdx.x >> 5);
-  if (w >= j.nwtiles) return;
-  const unsigned long long total =
-      ej_probe_count_warp_desc<EJ_TABLE_HASH, false, true>(j.S, w * PR_WTILE, j.nS, j.view, desc + j.desc0);
-  if ((threadIdx.x & 31u) == 0) wcount[j.first_wtile + w] = total;
-}
-
-// write pass: a warp tile's offset in its join's output is the scan of the
-// batch's warp-tile totals minus the scan at the join's first warp tile
+// one pass over every join's probe tiles (block = one 1024-probe tile of one
+// join): each warp reserves its rows on its join's cursor (d_count, zeroed
+// before the launch), so the cursor ends at the join's count
 __global__ void __launch_bounds__(PR_THREADS)
-batch_write_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles,
-                   const unsigned long long* __restrict__ woff, const uint2* __restrict__ desc, ej_dev_status* st) {
+batch_fused_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles, ej_dev_status* st) {
   __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
   const BatchPTile pt = ptiles[blockIdx.x];
   const BatchJoin& j = joins[pt.join];
-  const unsigned int warp = threadIdx.x >> 5;
+  const unsigned int warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   const uint64_t w = (uint64_t)pt.local * PR_WARPS + warp;
   if (w >= j.nwtiles) return;
-  const unsigned long long base = woff[j.first_wtile];
-  if (w == 0 && (threadIdx.x & 31u) == 0) {
-    const unsigned long long total = woff[j.first_wtile + j.nwtiles] - base;
-    *j.d_count = total;
-    if (total > j.cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  EjProbeWarp pw;
+  ej_probe_runs_warp<EJ_TABLE_HASH, false>(j.S, w * PR_WTILE, j.nS, j.view, pw);
+  unsigned long long mine = 0;
+#pragma unroll
+  for (int q = 0; q < PR_ITEMS; q++) mine += pw.cnt[q];
+  const unsigned long long total = ej_warp_sum<unsigned long long>(mine);
+  if (total == 0) return;
+  int32_t kk[PR_ITEMS][PW_PREFETCH];
+  ej_probe_prefetch(j.view, pw, kk);
+  unsigned long long off = 0;
+  if (lane == 0) {
+    off = atomicAdd(j.d_count, total);
+    if (off + total > j.cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
   }
-  const unsigned long long off = woff[j.first_wtile + w] - base;
+  off = __shfl_sync(EJ_FULL_MASK, off, 0);
   if (off >= j.cap) return;
-  ej_probe_write_warp(j.S, desc + j.desc0, w * PR_WTILE, j.nS, j.view, off, j.out, j.cap, stage[warp]);
+  ej_emit_warp(pw, kk, j.view, off, j.out, j.cap, stage[warp]);
 }
 
 }  // namespace
@@ -120,7 +111,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   std::vector<ej_rx_tile> rtiles;
   std::vector<BatchPTile> ptiles;
   std::vector<unsigned long long> sbase(n);
-  uint64_t nr_total = 0, start_total = 0, cells = 0, nw_total = 0, ns_total = 0;
+  uint64_t nr_total = 0, start_total = 0, cells = 0;
   for (uint32_t i = 0; i < n; i++) {
     const uint64_t nR = jd[i].nR, nS = jd[i].nS;
     BatchJoin& b = joins[i];
@@ -147,11 +138,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     cells += (uint64_t)rt * 256;
     sbase[i] = start_total;
     start_total += 1ull << b.view.hb;
-    b.first_wtile = nw_total;
     b.nwtiles = (nS + PR_WTILE - 1) / PR_WTILE;
-    nw_total += b.nwtiles;
-    b.desc0 = ns_total;
-    ns_total += nS;
     const uint32_t nptiles = (uint32_t)((nS + PR_TILE - 1) / PR_TILE);
     for (uint32_t t = 0; t < nptiles; t++) ptiles.push_back({i, t});
     nr_total += nR;
@@ -177,10 +164,6 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   rp.hist_off = p.add(cells * sizeof(uint32_t));
   rp.offs_off = p.add((cells + 1) * sizeof(uint32_t));
   rp.scan_off = p.add(ej_scan_scratch_bytes(cells));
-  const size_t wcount_off = p.add((nw_total + 1) * sizeof(unsigned long long));
-  const size_t woff_off = p.add((nw_total + 1) * sizeof(unsigned long long));
-  const size_t wscan_off = p.add(ej_scan_scratch_bytes(nw_total));
-  const size_t desc_off = p.add(std::max<uint64_t>(ns_total, 1) * sizeof(uint2));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
 
   char* A = static_cast<char*>(h->arena);
@@ -231,18 +214,11 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   }
   ej_phase_mark(h, 1);
   ej_phase_mark(h, 2);  // no partition pass: every table of a batch is probed in place
-  if (ptiles.empty()) ej_phase_mark(h, 3);
+  ej_phase_mark(h, 3);  // one pass: recorded as the write phase
   if (!ptiles.empty()) {
-    unsigned long long* wcount = reinterpret_cast<unsigned long long*>(A + wcount_off);
-    unsigned long long* woff = reinterpret_cast<unsigned long long*>(A + woff_off);
-    uint2* desc = reinterpret_cast<uint2*>(A + desc_off);
     const BatchPTile* dpt = reinterpret_cast<const BatchPTile*>(A + ptiles_off);
-    batch_count_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, wcount, desc);
-    EJ_TRY(ej_check_launch(h, "batch_count_kernel"));
-    EJ_TRY(ej_scan_u64_u64(h, wcount, nw_total, woff, A + wscan_off));
-    ej_phase_mark(h, 3);
-    batch_write_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, woff, desc, h->d_status);
-    EJ_TRY(ej_check_launch(h, "batch_write_kernel"));
+    batch_fused_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, h->d_status);
+    EJ_TRY(ej_check_launch(h, "batch_fused_kernel"));
   }
   ej_phase_mark(h, 4);
   return EJ_OK;

@@ -32,6 +32,7 @@
 #include <climits>
 
 #include "ej_device.cuh"
+#include "dir.cuh"
 #include "hash_join.cuh"
 #include "probe.cuh"
 #include "probe_write.cuh"
@@ -39,129 +40,34 @@
 namespace {
 
 
-// ---- key directory of a hash table ----------------------------------------
-// The distinct keys of the hash-sorted table, in hash order, each an entry
-// {hash, run start} placed by linear probing from its home slot
-// hash >> (32 - bits), 2^bits >= 2 x keys: key k goes to
-//   pos_k = max(home_k, pos_{k-1} + 1) = k + max_{j <= k} (home_j - j),
-// so the entries stay in hash order.  Every slot holds the first key at or
-// after it: the slots between pos_{k-1} and pos_k hold copies of key k, the
-// slots past the last entry a sentinel {0xFFFFFFFF, nR}.  A probe walks
-// forward from its home slot past smaller hashes; it has found its key when
-// the hash matches and the start is below nR, and the run ends at the first
-// later slot whose start differs (the next key's start).  The number of keys,
-// and so bits, is known only on the device: it lives in the header in front
-// of the entries.  Build: per 4096-row tile, count the rows that begin a key;
-// scan; per tile, the largest home_k - k; a prefix maximum over the tiles;
-// per tile, every key's slots (pos_{k-1}, pos_k]; then the slots before the
-// first entry and after the last.
-
-constexpr int DIR_ROWS = 16;              // consecutive rows per thread
-constexpr int DIR_TILE = 256 * DIR_ROWS;  // rows per block
-
-struct DirHeader {
-  uint32_t bits;
-  uint32_t hash0;  // hash of the first key
-  unsigned long long nkeys;
-  unsigned long long pos_first, pos_last;  // slots of the first and last entries
-};
-constexpr size_t DIR_HEADER_BYTES = 256;
-
-// DIR_ROWS consecutive rows of a thread: vals and which of them begin a key
-struct DirRows {
-  int32_t v[DIR_ROWS];
-  uint32_t f;  // bit e: row i0 + e begins a key
-};
-
-__device__ __forceinline__ void dir_rows(const int32_t* __restrict__ rval, uint64_t n, uint64_t i0, DirRows& r) {
-  r.f = 0;
-#pragma unroll
-  for (int e = 0; e < DIR_ROWS; e++) r.v[e] = 0;
-  if (i0 >= n) return;
-  // i0 is a multiple of DIR_ROWS; the column is 16-byte aligned and padded by
-  // 8 rows, so the vector loads past n that can happen stay inside it
-#pragma unroll
-  for (int q = 0; q < DIR_ROWS / 4; q++) {
-    if (i0 + 4u * q >= n) break;
-    const int4 x = *reinterpret_cast<const int4*>(rval + i0 + 4u * q);
-    r.v[4 * q] = x.x;
-    r.v[4 * q + 1] = x.y;
-    r.v[4 * q + 2] = x.z;
-    r.v[4 * q + 3] = x.w;
-  }
-  int32_t prev = i0 ? rval[i0 - 1] : 0;
-#pragma unroll
-  for (int e = 0; e < DIR_ROWS; e++) {
-    if (i0 + e < n && (i0 + e == 0 || r.v[e] != prev)) r.f |= 1u << e;
-    prev = r.v[e];
-  }
+// Row bounds of every bucket of the hash-sorted table (tables below
+// EJ_DIR_MIN_ROWS rows): row i (i = nR: the end) begins the buckets between
+// the bucket of row i - 1 and its own; each warp takes 256 consecutive rows.
+__global__ void __launch_bounds__(256)
+bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb) {
+  const uint64_t r0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * 256;
+  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket);
 }
 
-__device__ __forceinline__ uint32_t dir_bits_for(unsigned long long nk) {
-  uint32_t bits = 1;
-  while (bits < 32 && (1ull << bits) < 2 * nk) bits++;
-  return bits;
-}
+// ---- key directory of a single table (dir.cuh) -------------------------------
 
-// block-wide maximum scan, exclusive (LLONG_MIN for thread 0); *total = the block maximum
-__device__ __forceinline__ long long dir_block_exclusive_max(long long v, long long* tmp, long long* total) {
-  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  long long incl = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const long long u = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= (unsigned)o) incl = max(incl, u);
-  }
-  if (lane == 31u) tmp[warp] = incl;
-  __syncthreads();
-  long long before = LLONG_MIN;
-  for (unsigned w = 0; w < warp; w++) before = max(before, tmp[w]);
-  long long all = LLONG_MIN;
-  for (unsigned w = 0; w < nw; w++) all = max(all, tmp[w]);
-  const long long up = __shfl_up_sync(0xffffffffu, incl, 1);
-  const long long ex = max(before, lane ? up : LLONG_MIN);
-  __syncthreads();
-  *total = all;
-  return ex;
-}
-
-// rows beginning a key, per tile
-__global__ void __launch_bounds__(256) dir_count_kernel(const int32_t* __restrict__ rval, uint64_t n,
-                                                        uint32_t* __restrict__ tile_keys) {
-  __shared__ uint32_t tmp[256 / 32 + 1];
-  DirRows r;
-  dir_rows(rval, n, (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS, r);
-  uint32_t total;
-  ej_block_exclusive_sum<256, uint32_t>((uint32_t)__popc(r.f), tmp, &total);
+__global__ void __launch_bounds__(DIR_THREADS) dir_count_kernel(const int32_t* __restrict__ rval, uint64_t n,
+                                                                uint32_t* __restrict__ tile_keys) {
+  const uint32_t total = dir_tile_keys(rval, n, (uint64_t)blockIdx.x * DIR_TILE);
   if (threadIdx.x == 0) tile_keys[blockIdx.x] = total;
 }
 
 // per tile: the largest home_k - k; the header (key count, bits, first hash)
-__global__ void __launch_bounds__(256) dir_tilemax_kernel(const int32_t* __restrict__ rval, uint64_t n,
-                                                          const uint32_t* __restrict__ tile_off, uint32_t ntiles,
-                                                          long long* __restrict__ kmax, DirHeader* hdr) {
-  __shared__ uint32_t tmp[256 / 32 + 1];
-  __shared__ long long tmpl[256 / 32];
-  const uint64_t i0 = (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS;
-  DirRows r;
-  dir_rows(rval, n, i0, r);
-  uint32_t total;
-  uint64_t k = tile_off[blockIdx.x] + ej_block_exclusive_sum<256, uint32_t>((uint32_t)__popc(r.f), tmp, &total);
+__global__ void __launch_bounds__(DIR_THREADS) dir_tilemax_kernel(const int32_t* __restrict__ rval, uint64_t n,
+                                                                  const uint32_t* __restrict__ tile_off,
+                                                                  uint32_t ntiles, long long* __restrict__ kmax,
+                                                                  DirHeader* hdr) {
   const unsigned long long nk = tile_off[ntiles];
-  const uint32_t bits = dir_bits_for(nk), shift = 32u - bits;
-  long long m = LLONG_MIN;
-#pragma unroll
-  for (int e = 0; e < DIR_ROWS; e++)
-    if (r.f >> e & 1u) {
-      m = max(m, (long long)(ej_hash32((uint32_t)r.v[e]) >> shift) - (long long)k);
-      k++;
-    }
-  long long all;
-  dir_block_exclusive_max(m, tmpl, &all);
-  if (threadIdx.x == 0) kmax[blockIdx.x] = all;
+  const uint32_t bits = dir_bits_for(nk);
+  const long long m = dir_tile_max(rval, n, (uint64_t)blockIdx.x * DIR_TILE, tile_off[blockIdx.x], bits, &hdr->hash0);
+  if (threadIdx.x == 0) kmax[blockIdx.x] = m;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     hdr->bits = bits;
-    hdr->hash0 = ej_hash32((uint32_t)r.v[0]);  // row 0 begins the first key
     hdr->nkeys = nk;
   }
 }
@@ -195,63 +101,16 @@ __global__ void __launch_bounds__(1024) dir_prefix_kernel(const long long* __res
   }
 }
 
-// per tile: every key's slots (pos_{k-1}, pos_k], holding {hash_k, start_k}
-__global__ void __launch_bounds__(256) dir_place_kernel(const int32_t* __restrict__ rval, uint64_t n,
-                                                        const uint32_t* __restrict__ tile_off,
-                                                        const long long* __restrict__ kpre, DirHeader* hdr,
-                                                        uint2* __restrict__ dir) {
-  __shared__ uint32_t tmp[256 / 32 + 1];
-  __shared__ long long tmpl[256 / 32];
-  const uint64_t i0 = (uint64_t)blockIdx.x * DIR_TILE + threadIdx.x * DIR_ROWS;
-  DirRows r;
-  dir_rows(rval, n, i0, r);
-  uint32_t total;
-  uint64_t k = tile_off[blockIdx.x] + ej_block_exclusive_sum<256, uint32_t>((uint32_t)__popc(r.f), tmp, &total);
-  const unsigned long long nk = hdr->nkeys;
-  const uint32_t shift = 32u - hdr->bits;
-  long long m = LLONG_MIN;
-  uint64_t kk = k;
-#pragma unroll
-  for (int e = 0; e < DIR_ROWS; e++)
-    if (r.f >> e & 1u) {
-      m = max(m, (long long)(ej_hash32((uint32_t)r.v[e]) >> shift) - (long long)kk);
-      kk++;
-    }
-  long long all;
-  long long run = max(kpre[blockIdx.x], dir_block_exclusive_max(m, tmpl, &all));  // max over keys before k
-  long long prev = k ? (long long)k - 1 + run : -1;                                // pos_{k-1}
-#pragma unroll
-  for (int e = 0; e < DIR_ROWS; e++) {
-    if (!(r.f >> e & 1u)) continue;
-    const uint32_t hv = ej_hash32((uint32_t)r.v[e]);
-    run = max(run, (long long)(hv >> shift) - (long long)k);
-    const long long pos = (long long)k + run;
-    const uint2 entry = make_uint2(hv, (uint32_t)(i0 + e));
-    // key 0's leading slots [0, pos_0) are written by dir_edge_kernel
-    for (long long g = (k ? prev + 1 : pos); g <= pos; g++) dir[g] = entry;
-    if (k == 0) hdr->pos_first = (unsigned long long)pos;
-    if (k + 1 == nk) hdr->pos_last = (unsigned long long)pos;
-    prev = pos;
-    k++;
-  }
+__global__ void __launch_bounds__(DIR_THREADS) dir_place_kernel(const int32_t* __restrict__ rval, uint64_t n,
+                                                                const uint32_t* __restrict__ tile_off,
+                                                                const long long* __restrict__ kpre, DirHeader* hdr,
+                                                                uint2* __restrict__ dir) {
+  dir_tile_place(rval, n, (uint64_t)blockIdx.x * DIR_TILE, tile_off[blockIdx.x], kpre[blockIdx.x], hdr, dir);
 }
 
-// the slots before the first entry (copies of the first key) and from one
-// past the last entry to 2^bits + 1, at least two of them (sentinels
-// {0xFFFFFFFF, n}; a probe reads the slot after the one it stops at); with no
-// keys, slots [0, 2^bits + 1]
 __global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restrict__ hdr, uint64_t n,
                                                        uint2* __restrict__ dir) {
-  const unsigned long long home_end = 1ull << hdr->bits;
-  const bool any = hdr->nkeys != 0;
-  const unsigned long long first = any ? hdr->pos_first : 0ull;
-  const unsigned long long tail = any ? hdr->pos_last + 1 : 0ull;
-  const unsigned long long tail_end = max(home_end, tail) + 2;
-  const uint2 lead = make_uint2(hdr->hash0, 0u), sentinel = make_uint2(0xFFFFFFFFu, (uint32_t)n);
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < first; i += stride) dir[i] = lead;
-  for (uint64_t i = tail + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tail_end; i += stride)
-    dir[i] = sentinel;
+  dir_edges(hdr, n, dir, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
 }
 
 // fence[i] = rval[i * EJ_FENCE_STRIDE] of a val-sorted table
@@ -361,18 +220,10 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta) {
 
 // ---- table build --------------------------------------------------------
 
-// directory slots reserved for nR rows: 2^bits <= next power of two of 2 nR,
-// plus one slot per key for the entries past the last home slot, plus two
-// sentinels (the last written slot is at most 2^bits + keys)
-static uint64_t ej_dir_capacity(uint64_t nR) {
-  uint64_t p = 2;
-  while (p < 2 * nR) p <<= 1;
-  return p + nR + 2;
-}
 
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
-  return tp.kind == EJ_TABLE_HASH ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint2)
-                                  : (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
+  if (tp.kind != EJ_TABLE_HASH) return (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
+  return tp.use_dir ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint2) : (size_t(1) << tp.hb) * sizeof(uint2);
 }
 
 size_t ej_table_col_bytes(uint64_t nR) { return (size_t)(nR + EJ_TABLE_PAD) * sizeof(int32_t); }
@@ -380,6 +231,7 @@ size_t ej_table_col_bytes(uint64_t nR) { return (size_t)(nR + EJ_TABLE_PAD) * si
 void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta) {
   tp.kind = kind;
   tp.nR = nR;
+  tp.use_dir = kind == EJ_TABLE_HASH && nR >= EJ_DIR_MIN_ROWS;
   tp.hb = kind == EJ_TABLE_HASH ? ej_table_bucket_bits(nR, delta) : 32u;
   tp.passes = 4;  // all 32 key bits: equal keys end up adjacent
   tp.nfence = (uint32_t)((nR + EJ_FENCE_STRIDE - 1) / EJ_FENCE_STRIDE);
@@ -392,7 +244,7 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
   tp.tmp_a_off = p.add(tuples);
   tp.tmp_b_off = p.add(tuples);
   ej_radix_plan_add(p, tp.rplan, nR);
-  if (kind == EJ_TABLE_HASH) {  // directory build scratch
+  if (tp.use_dir) {  // directory build scratch
     const uint64_t tiles = (nR + DIR_TILE - 1) / DIR_TILE + 1;
     tp.dir_keys_off = p.add(tiles * sizeof(uint32_t));
     tp.dir_off_off = p.add((tiles + 1) * sizeof(uint32_t));
@@ -433,7 +285,13 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
   view->rval = rval;
   view->nR = tp.nR;
   view->hb = tp.hb;
-  if (tp.kind == EJ_TABLE_HASH) {
+  if (tp.kind == EJ_TABLE_HASH && !tp.use_dir) {
+    uint2* bucket = static_cast<uint2*>(aux);
+    const uint64_t blocks = (tp.nR + 1 + 2047) / 2048;  // 256 rows per warp, 8 warps per block
+    bucket_start_kernel<<<(unsigned)blocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb);
+    EJ_TRY(ej_check_launch(h, "bucket_start_kernel"));
+    view->bucket = bucket;
+  } else if (tp.kind == EJ_TABLE_HASH) {
     DirHeader* hdr = static_cast<DirHeader*>(aux);
     uint2* dir = reinterpret_cast<uint2*>(static_cast<char*>(aux) + DIR_HEADER_BYTES);
     const uint32_t tiles = (uint32_t)((tp.nR + DIR_TILE - 1) / DIR_TILE);

@@ -7,8 +7,14 @@
 
 #include "ej_internal.h"
 
+// Hash tables of at least this many rows carry a key directory (one load per
+// probe, seven build launches); smaller ones carry bucket bounds (one build
+// launch; the bucket scan costs nothing extra while the table sits in L2)
+constexpr uint64_t EJ_DIR_MIN_ROWS = 1ull << 20;
+
 struct ej_table_plan_t {
   int kind = EJ_TABLE_HASH;
+  bool use_dir = false;  // hash tables: key directory (else bucket bounds)
   uint64_t nR = 0;
   uint32_t hb = 1;      // bucket bits (hash tables)
   uint32_t passes = 4;  // LSD radix passes over the 32-bit key
