@@ -276,7 +276,8 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
     """A small case for profilers: `repeat` hash joins of one workload at
     1/2^scale size, each synchronised; prints the phase times of the last.
     d2 / d3: `repeat` distance joins of 2^(19 - scale) x 2^(19 - scale) points
-    (after one count-only call)."""
+    (after one count-only call); c5_batch: `repeat` batches of the served
+    stream's 256 request instances."""
     import torch
 
     from eating_one_gb300.build import build
@@ -285,6 +286,20 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
 
     build()
     eng = Engine(0)
+    if name == "c5_batch":  # the served stream's 256 request instances as one batch per call
+        from eating_one_gb300 import native
+        from eating_one_gb300.serve import RequestPool
+
+        pool = RequestPool(eng, 256)
+        descs = (native.JoinDesc * len(pool.desc))(*pool.desc)
+        d_counts = torch.zeros(len(pool.desc), dtype=torch.int64, device="cuda")
+        for _ in range(repeat):
+            eng.batch_hash_join_async(descs, len(pool.desc), d_counts)
+        torch.cuda.synchronize()
+        got = d_counts.cpu().tolist()
+        assert got == pool.expected
+        print(json.dumps({"profile_case": name, "joins": len(got), "rows": int(sum(got))}), flush=True)
+        return
     if name in ("d2", "d3"):  # distance joins: dist_screen_kernel x2 + dist_kernel per call
         from eating_one_gb300.native import point_result_dtype
         from eating_one_gb300.workloads import distance_workload
