@@ -100,16 +100,30 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
         }
       }
     }
+    // the N walks advance together, one slot per round, so that a warp waits
+    // for as many dependent loads as its longest walk, not for their sum
+    uint32_t walk = 0;
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      if (ok[j] && a[j].x < hv[j]) walk |= 1u << j;
+    while (walk) {
+#pragma unroll
+      for (int j = 0; j < N; j++)
+        if (walk & (1u << j)) {
+          a[j] = b[j];
+          b[j] = __ldg(t.dir + ++slot[j] + 1);
+        }
+#pragma unroll
+      for (int j = 0; j < N; j++)
+        if ((walk & (1u << j)) && a[j].x >= hv[j]) walk &= ~(1u << j);
+    }
 #pragma unroll
     for (int j = 0; j < N; j++) {
       lo[j] = 0u;
       c[j] = 0u;
-      if (!ok[j]) continue;
-      while (a[j].x < hv[j]) {
-        a[j] = b[j];
-        b[j] = __ldg(t.dir + ++slot[j] + 1);
-      }
-      if (a[j].x != hv[j] || a[j].y >= t.nR) continue;
+      if (!ok[j] || a[j].x != hv[j] || a[j].y >= t.nR) continue;
+      // a present key's home slot is never a gap, so the walk stops at the
+      // key's own slot and the next slot starts another run; the loop is a guard
       while (b[j].y == a[j].y) b[j] = __ldg(t.dir + ++slot[j] + 1);
       lo[j] = a[j].y;
       c[j] = b[j].y - a[j].y;
