@@ -412,7 +412,7 @@ template <int KIND, bool OUTER>
 static ej_status launch_fused(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                               unsigned long long* cursor, ej_result* out, uint64_t cap) {
   probe_fused_kernel<KIND, OUTER><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(
-      P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 4 * PR_WARPS);
+      P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 32);
   return ej_check_launch(h, "probe_fused_kernel");
 }
 

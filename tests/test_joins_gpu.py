@@ -88,11 +88,28 @@ def test_extreme_keys(engine):
         same_multiset(engine.join(algo, dev(R), dev(S)), ORACLE[algo](R, S))
 
 
-@pytest.mark.parametrize("pb", [1, 3, 6, 8])
+@pytest.mark.parametrize("pb", [1, 3, 6, 7, 8])
 def test_partitioned_probe(engine, pb):
     """Force the S radix-partition pass (taken automatically only for tables beyond L2)."""
     rng = np.random.default_rng(pb)
     R, S = rel(rng, 50000, 0, 30000), rel(rng, 200003, 0, 40000, key_base=50000)
+    engine.set_option("partition_bits", pb)
+    try:
+        got_hash = engine.join("hash", dev(R), dev(S))
+        got_outer = engine.join("left_outer", dev(R), dev(S))
+    finally:
+        engine.set_option("partition_bits", -1)
+    same_multiset(got_hash, O.hash_join(R, S))
+    same_multiset(got_outer, O.left_outer_join(R, S))
+
+
+@pytest.mark.parametrize("pb", [5, 7])
+def test_partitioned_probe_skewed(engine, pb):
+    """One partition holds 90% of S: its (partition, group) segments span many warp tiles."""
+    rng = np.random.default_rng(100 + pb)
+    R = rel(rng, 40000, 0, 20000)
+    S = rel(rng, 150001, 0, 25000, key_base=40000)
+    S[rng.random(len(S)) < 0.9, 1] = R[7, 1]
     engine.set_option("partition_bits", pb)
     try:
         got_hash = engine.join("hash", dev(R), dev(S))
