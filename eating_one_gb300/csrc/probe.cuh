@@ -158,6 +158,8 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
       if (base + 4 < s1[j]) qb[j] = __ldg(rv4 + base / 4 + 1);
     }
   }
+  uint32_t more = 0;  // bit j: the run or the search of probe j goes on past the 8 loaded values
+  uint32_t next[N];   // the next 4 values to scan
 #pragma unroll
   for (int j = 0; j < N; j++) {
     // equality mask of the 8 loaded values, restricted to the bucket
@@ -174,14 +176,26 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
     lo[j] = c[j] ? base + (uint32_t)(__ffs(eq) - 1) : s1[j];
     // a run goes on past the 8 loaded values only if it reaches their end; with
     // no match yet, the search goes on only if the bucket does
-    bool ended = c[j] ? !(eq & 0x80u) : (to < 8u);
-    for (uint32_t i = base + 8; i < s1[j] && !ended; i += 4) {
-      const int4 q = __ldg(rv4 + i / 4);
-      const int y[4] = {q.x, q.y, q.z, q.w};
+    const bool ended = c[j] ? !(eq & 0x80u) : (to < 8u);
+    next[j] = base + 8;
+    if (!ended && next[j] < s1[j]) more |= 1u << j;
+  }
+  // the N scans advance together, 4 values per round, so that a warp waits
+  // for as many dependent loads as its longest scan, not for their sum
+  while (more) {
+    int4 q[N];
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      if (more & (1u << j)) q[j] = __ldg(rv4 + next[j] / 4);
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      if (!(more & (1u << j))) continue;
+      const int y[4] = {q[j].x, q[j].y, q[j].z, q[j].w};
+      bool ended = false;
 #pragma unroll
       for (int e = 0; e < 4; e++) {
-        const uint32_t idx = i + (uint32_t)e;
-        if (idx >= s1[j]) continue;
+        const uint32_t idx = next[j] + (uint32_t)e;
+        if (idx >= s1[j] || ended) continue;
         if (y[e] == v[j]) {
           if (c[j] == 0) lo[j] = idx;
           c[j]++;
@@ -189,9 +203,12 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
           ended = true;
         }
       }
+      next[j] += 4;
+      if (ended || next[j] >= s1[j]) more &= ~(1u << j);
     }
-    lo[j] -= t.voff;
   }
+#pragma unroll
+  for (int j = 0; j < N; j++) lo[j] -= t.voff;
 }
 
 template <>
