@@ -69,7 +69,7 @@ __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, 
   // tiles are multiples of 256 rows except a join's last, so a warp's 256
   // rows never reach into the next tile
   for (uint64_t r0 = first + (threadIdx.x >> 5) * 256; r0 < end; r0 += (blockDim.x >> 5) * 256)
-    ej_bucket_bounds_warp(t.rval, t.nR, r0, t.hb, bucket);
+    ej_bucket_bounds_warp(t.rval, t.nR, r0, t.hb, bucket, EjHashBucketOf{t.hb});
 }
 
 // one pass over every join's probe tiles (block = one 1024-probe tile of one

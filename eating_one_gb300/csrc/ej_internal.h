@@ -157,11 +157,11 @@ ej_status ej_radix_pass_soa(ej_handle* h, const ej_radix_plan& rp, const ej_tupl
 // EJ_TABLE_HASH: sorted by hash32(val), so equal keys form one contiguous run
 //   and bucket b (top `hb` hash bits) is rows [bucket[b].x, bucket[b].y)
 //   (both bounds in one 8-byte word, so a probe reads them with one load).
-// EJ_TABLE_SORTED: sorted by val; the run of a value is found by binary
-//   search, narrowed first by a fence of every 256th val.
+// EJ_TABLE_SORTED: sorted by val; bucket b of value v = (v - vmin) >> vshift
+//   is rows [bucket[b].x, bucket[b].y), with vmin, vmax and vshift in a
+//   16-byte device header (vbuckets) written after the sort.
 // Both arrays carry EJ_TABLE_PAD readable elements past nR (vector loads).
 enum { EJ_TABLE_HASH = 0, EJ_TABLE_SORTED = 1 };
-constexpr uint32_t EJ_FENCE_STRIDE = 256;
 constexpr uint64_t EJ_TABLE_PAD = 8;
 struct ej_table_view {
   int kind = EJ_TABLE_HASH;
@@ -170,10 +170,9 @@ struct ej_table_view {
   const uint2* bucket = nullptr;     // [2^hb] (hash, batched tables): row bounds of each bucket
   const uint2* dir = nullptr;        // (hash, single tables) key directory {hash, run start}
   const uint32_t* dir_bits = nullptr;  // device word: the directory has 2^bits home slots
-  const int32_t* fence = nullptr;    // [nfence] (sorted)
+  const void* vbuckets = nullptr;    // (sorted) device EjValueBuckets {vmin, vmax, vshift} of `bucket`
   uint64_t nR = 0;
   uint32_t hb = 1;
-  uint32_t nfence = 0;
   uint32_t voff = 0;  // rval - voff is 16-byte aligned (tables of a batch share one array)
 };
 uint32_t ej_table_bucket_bits(uint64_t nR, int delta = 0);

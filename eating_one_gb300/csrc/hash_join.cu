@@ -46,7 +46,7 @@ namespace {
 __global__ void __launch_bounds__(256)
 bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb) {
   const uint64_t r0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * 256;
-  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket);
+  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket, EjHashBucketOf{hb});
 }
 
 // ---- key directory of a single table (dir.cuh) -------------------------------
@@ -113,10 +113,28 @@ __global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restri
   dir_edges(hdr, n, dir, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
 }
 
-// fence[i] = rval[i * EJ_FENCE_STRIDE] of a val-sorted table
-__global__ void fence_kernel(const int32_t* __restrict__ rval, int32_t* __restrict__ fence, uint32_t nfence) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nfence; i += gridDim.x * blockDim.x)
-    fence[i] = rval[(uint64_t)i * EJ_FENCE_STRIDE];
+// the value buckets of a val-sorted table of n rows (2^hb buckets): the
+// smallest and largest vals and the shift that maps their range below 2^hb
+__global__ void vbucket_header_kernel(const int32_t* __restrict__ rval, uint64_t n, uint32_t hb,
+                                      EjValueBuckets* __restrict__ hdr) {
+  EjValueBuckets b = {1, 0, 0u, 0u};  // no rows: an empty range
+  if (n) {
+    b.vmin = rval[0];
+    b.vmax = rval[n - 1];
+    const uint32_t range = (uint32_t)b.vmax - (uint32_t)b.vmin;
+    const uint32_t len = range ? 32u - (uint32_t)__clz(range) : 0u;
+    b.vshift = len > hb ? len - hb : 0u;
+  }
+  *hdr = b;
+}
+
+// bounds of the value buckets: rows [r0, r0 + 256) per warp
+__global__ void __launch_bounds__(256)
+vbucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb,
+                     const EjValueBuckets* __restrict__ hdr) {
+  const uint64_t r0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * 256;
+  const EjValueBuckets b = *hdr;
+  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket, EjValueBucketOf{b.vmin, b.vshift});
 }
 
 // ---- count, then write from the run descriptors ---------------------------------
@@ -222,7 +240,7 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta) {
 
 
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
-  if (tp.kind != EJ_TABLE_HASH) return (size_t)(tp.nfence ? tp.nfence : 1) * sizeof(int32_t);
+  if (tp.kind != EJ_TABLE_HASH) return EJ_VBUCKET_HEADER_BYTES + (size_t(1) << tp.hb) * sizeof(uint2);
   return tp.use_dir ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint2) : (size_t(1) << tp.hb) * sizeof(uint2);
 }
 
@@ -232,9 +250,8 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
   tp.kind = kind;
   tp.nR = nR;
   tp.use_dir = kind == EJ_TABLE_HASH && nR >= EJ_DIR_MIN_ROWS;
-  tp.hb = kind == EJ_TABLE_HASH ? ej_table_bucket_bits(nR, delta) : 32u;
+  tp.hb = ej_table_bucket_bits(nR, delta);  // hash buckets, or value buckets of a sorted table
   tp.passes = 4;  // all 32 key bits: equal keys end up adjacent
-  tp.nfence = (uint32_t)((nR + EJ_FENCE_STRIDE - 1) / EJ_FENCE_STRIDE);
   if (!own_storage) {
     tp.rkey_off = p.add(ej_table_col_bytes(nR));
     tp.rval_off = p.add(ej_table_col_bytes(nR));
@@ -317,15 +334,16 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
     EJ_TRY(ej_check_launch(h, "dir_edge_kernel"));
     view->dir = dir;
     view->dir_bits = &hdr->bits;
-  } else {
-    int32_t* fence = static_cast<int32_t*>(aux);
-    if (tp.nfence) {
-      const unsigned blocks = (unsigned)std::min<uint64_t>((tp.nfence + 255) / 256, (uint64_t)h->num_sms * 16);
-      fence_kernel<<<blocks, 256, 0, h->stream>>>(rval, fence, tp.nfence);
-      EJ_TRY(ej_check_launch(h, "fence_kernel"));
-    }
-    view->fence = fence;
-    view->nfence = tp.nfence;
+  } else {  // sorted: value buckets, header first
+    EjValueBuckets* vh = static_cast<EjValueBuckets*>(aux);
+    uint2* bucket = reinterpret_cast<uint2*>(static_cast<char*>(aux) + EJ_VBUCKET_HEADER_BYTES);
+    vbucket_header_kernel<<<1, 1, 0, h->stream>>>(rval, tp.nR, tp.hb, vh);
+    EJ_TRY(ej_check_launch(h, "vbucket_header_kernel"));
+    const uint64_t blocks = (tp.nR + 1 + 2047) / 2048;  // 256 rows per warp, 8 warps per block
+    vbucket_start_kernel<<<(unsigned)blocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb, vh);
+    EJ_TRY(ej_check_launch(h, "vbucket_start_kernel"));
+    view->bucket = bucket;
+    view->vbuckets = vh;
   }
   return EJ_OK;
 }

@@ -11,14 +11,15 @@
 // probe, seven build launches); smaller ones carry bucket bounds (one build
 // launch; the bucket scan costs nothing extra while the table sits in L2)
 constexpr uint64_t EJ_DIR_MIN_ROWS = 1ull << 20;
+// a sorted table's aux storage: the value buckets' header, then the bounds
+constexpr size_t EJ_VBUCKET_HEADER_BYTES = 256;
 
 struct ej_table_plan_t {
   int kind = EJ_TABLE_HASH;
   bool use_dir = false;  // hash tables: key directory (else bucket bounds)
   uint64_t nR = 0;
-  uint32_t hb = 1;      // bucket bits (hash tables)
+  uint32_t hb = 1;      // bucket bits (hash buckets, or value buckets of a sorted table)
   uint32_t passes = 4;  // LSD radix passes over the 32-bit key
-  uint32_t nfence = 0;  // sorted index: fence entries
   // arena offsets; rkey/rval/aux are unused when the table has its own storage
   size_t rkey_off = 0, rval_off = 0, aux_off = 0, tmp_a_off = 0, tmp_b_off = 0;
   // key directory build scratch (hash tables)
@@ -45,7 +46,8 @@ struct ej_probe_layout {
 size_t ej_table_bytes(uint64_t nR, int delta = 0);
 // bytes of one column (rkey or rval) including the vector-load padding
 size_t ej_table_col_bytes(uint64_t nR);
-// bytes of the bucket starts (hash) or the fence (sorted)
+// bytes of the bucket bounds or the key directory (hash), or the value
+// buckets and their header (sorted)
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp);
 void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta = 0);
 ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, int32_t* rkey, int32_t* rval,

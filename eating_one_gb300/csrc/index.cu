@@ -7,9 +7,11 @@
 // inner-idx-bnlj.cc:175-217, recursive quicksort of BUCKET{val,adr}), then
 // probes one S tuple per thread (count.cu:16-48 / join_gpu.cu:8-86;
 // sort_index join_gpu.cu:10-113).  Here both indexes are built on the device
-// with the LSD radix passes of radix.cu: the hash index is the bucketised
-// table of hash_join.cu, the sort index is R sorted stably by val plus a fence
-// of every 256th val that narrows the binary search to one 2 KB segment.
+// with the LSD radix passes of radix.cu: the hash index is the table of
+// hash_join.cu (key directory or bucket bounds), the sort index is R sorted by
+// val with bucket bounds over value prefixes, (v - vmin) >> vshift, so that a
+// probe reads one 8-byte bound pair and the first 8 vals of its bucket
+// instead of two binary searches over the table (probe.cuh).
 #include "ej_device.cuh"
 #include "ej_entry.h"
 #include "hash_join.cuh"
@@ -21,7 +23,7 @@ struct ej_index {
   uint64_t nR = 0;
   int32_t* rkey = nullptr;  // device, owned
   int32_t* rval = nullptr;  // device, owned
-  void* aux = nullptr;      // device, owned: bucket starts or fence
+  void* aux = nullptr;      // device, owned: key directory, bucket bounds or value buckets
   ej_table_view view;
 };
 
@@ -96,13 +98,11 @@ static ej_status index_probe(ej_handle* h, const ej_index* ix, const ej_tuple* S
     EJ_TRY(ej_check_out(h, out, cap, out_count));
   }
   // hash index: partition S by hash when the index outgrows L2; a sorted
-  // index is probed in place (its fence keeps the search top in L2)
+  // index is probed in place (S in hash partitions would not follow its order)
   const uint32_t pb = ix->kind == EJ_TABLE_HASH ? ej_probe_partition_bits(h, ix->nR, nS) : 0u;
   ej_plan_bytes p;
   ej_probe_layout L;
-  // a sorted index's run search (two binary searches) is long: it runs once,
-  // in the count pass, and the write pass reads the run descriptors
-  ej_probe_layout_add(p, L, nS, pb, count_only, /*two_pass=*/ix->kind == EJ_TABLE_SORTED);
+  ej_probe_layout_add(p, L, nS, pb, count_only);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_phase_mark(h, 1);

@@ -169,6 +169,20 @@ def test_capacity_and_guard(engine):
     assert engine.count("hash", dev(R), dev(S)) == total
 
 
+def test_wide_buckets(engine):
+    """Two outliers stretch the value range, so a sorted index's value buckets
+    hold tens of thousands of distinct vals (runs found by binary search past
+    the first 8 values of a bucket); the same relation in a hash table."""
+    rng = np.random.default_rng(21)
+    R = rel(rng, 50000, 0, 50000)
+    R[0, 1], R[1, 1] = INT_MIN, INT_MAX
+    R[2:400, 1] = 777  # one long run inside the dense cluster
+    S = rel(rng, 60000, -10, 50010, key_base=50000)
+    S[:5, 1] = [INT_MIN, INT_MAX, 777, INT_MIN + 1, INT_MAX - 1]
+    for algo in ("sort_index", "hash_index", "hash", "left_outer"):
+        same_multiset(engine.join(algo, dev(R), dev(S)), ORACLE[algo](R, S))
+
+
 def test_index_reuse_and_count(engine):
     rng = np.random.default_rng(5)
     R = rel(rng, 40000, 0, 20000)
