@@ -277,7 +277,8 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
     1/2^scale size, each synchronised; prints the phase times of the last.
     d2 / d3: `repeat` distance joins of 2^(19 - scale) x 2^(19 - scale) points
     (after one count-only call); c5_batch: `repeat` batches of the served
-    stream's 256 request instances."""
+    stream's 256 request instances; c4_index: `repeat` times a hash index and a
+    sort index built on C4's R and probed with its S."""
     import torch
 
     from eating_one_gb300.build import build
@@ -299,6 +300,21 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
         got = d_counts.cpu().tolist()
         assert got == pool.expected
         print(json.dumps({"profile_case": name, "joins": len(got), "rows": int(sum(got))}), flush=True)
+        return
+    if name == "c4_index":  # per repeat: a hash index and a sort index built on C4's R, each probed once
+        w = workload("c4", scale)
+        R, S = eng.generate(w["R"]), eng.generate(w["S"])
+        n_out = eng.count("hash", R, S)
+        out = torch.empty((n_out, 4), dtype=torch.int32, device="cuda")
+        for _ in range(repeat):
+            for kind in ("hash", "sort"):
+                ix = eng.build_index(kind, R)
+                try:
+                    assert ix.join(S, out=out).shape[0] == n_out
+                finally:
+                    ix.free()
+        print(json.dumps({"profile_case": name, "scale": scale, "R": int(R.shape[0]), "S": int(S.shape[0]),
+                          "rows": n_out}), flush=True)
         return
     if name in ("d2", "d3"):  # distance joins: dist_screen_kernel x2 + dist_kernel per call
         from eating_one_gb300.native import point_result_dtype

@@ -124,6 +124,7 @@ extern "C" ej_status ej_trim(ej_handle* h) {
   EJ_CUDA(h, cudaFree(h->stage));
   h->arena = h->stage = nullptr;
   h->arena_cap = h->stage_cap = 0;
+  ej_index_pool_trim(h->device);
   return EJ_OK;
 }
 

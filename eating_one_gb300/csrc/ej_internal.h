@@ -82,6 +82,8 @@ ej_status ej_bnl_append(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_t
 ej_status ej_arena_reserve(ej_handle* h, size_t bytes);
 inline char* ej_arena_at(ej_handle* h, size_t off) { return static_cast<char*>(h->arena) + off; }
 ej_status ej_check_launch(ej_handle* h, const char* what);
+// the index memory pool of a device gives back the memory no index holds (index.cu)
+void ej_index_pool_trim(int device);
 // phase timing: begin a join's event set (mark 0), then marks 1..EJ_PHASES at
 // the phase boundaries (build | partition | count | write); no-ops when timing is off
 void ej_phase_begin(ej_handle* h);

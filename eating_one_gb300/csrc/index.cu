@@ -12,6 +12,9 @@
 // val with bucket bounds over value prefixes, (v - vmin) >> vshift, so that a
 // probe reads one 8-byte bound pair and the first 8 vals of its bucket
 // instead of two binary searches over the table (probe.cuh).
+#include <map>
+#include <mutex>
+
 #include "ej_device.cuh"
 #include "ej_entry.h"
 #include "hash_join.cuh"
@@ -27,10 +30,48 @@ struct ej_index {
   ej_table_view view;
 };
 
-static void index_release(ej_index* ix) {
-  cudaFree(ix->rkey);
-  cudaFree(ix->rval);
-  cudaFree(ix->aux);
+// Index storage comes from a stream-ordered memory pool per device that keeps
+// freed memory for the next index (its release threshold is unlimited), so an
+// index built after another was freed costs no cudaMalloc (which maps fresh
+// pages and synchronises the device: about half of a 2^24-row index build);
+// ej_trim returns the pool's unused memory.
+static std::mutex g_pool_mu;
+static std::map<int, cudaMemPool_t> g_pools;
+
+static cudaError_t index_pool(int device, cudaMemPool_t* pool) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  auto it = g_pools.find(device);
+  if (it != g_pools.end()) {
+    *pool = it->second;
+    return cudaSuccess;
+  }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  cudaError_t e = cudaMemPoolCreate(pool, &props);
+  if (e != cudaSuccess) return e;
+  uint64_t keep = UINT64_MAX;
+  e = cudaMemPoolSetAttribute(*pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (e != cudaSuccess) {
+    cudaMemPoolDestroy(*pool);
+    return e;
+  }
+  g_pools[device] = *pool;
+  return cudaSuccess;
+}
+
+void ej_index_pool_trim(int device) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  auto it = g_pools.find(device);
+  if (it != g_pools.end()) cudaMemPoolTrimTo(it->second, 0);
+}
+
+// the index's storage back to the pool, ordered on `stream`
+static void index_release(ej_index* ix, cudaStream_t stream) {
+  if (ix->rkey) cudaFreeAsync(ix->rkey, stream);
+  if (ix->rval) cudaFreeAsync(ix->rval, stream);
+  if (ix->aux) cudaFreeAsync(ix->aux, stream);
   delete ix;
 }
 
@@ -50,10 +91,13 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
   ix->device = h->device;
   ix->nR = nR;
   const size_t col = ej_table_col_bytes(nR), aux_bytes = ej_table_aux_bytes(tp);
-  if (cudaMalloc(&ix->rkey, col) != cudaSuccess || cudaMalloc(&ix->rval, col) != cudaSuccess ||
-      cudaMalloc(&ix->aux, aux_bytes) != cudaSuccess) {
+  cudaMemPool_t pool;
+  if (index_pool(h->device, &pool) != cudaSuccess ||
+      cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ix->rkey), col, pool, h->stream) != cudaSuccess ||
+      cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ix->rval), col, pool, h->stream) != cudaSuccess ||
+      cudaMallocFromPoolAsync(&ix->aux, aux_bytes, pool, h->stream) != cudaSuccess) {
     cudaGetLastError();
-    index_release(ix);
+    index_release(ix, h->stream);
     return ej_fail(h, EJ_ERR_NOMEM, "index storage of %zu bytes could not be allocated", 2 * col + aux_bytes);
   }
   ej_phase_begin(h);
@@ -61,7 +105,8 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
   for (int k = 1; k <= EJ_PHASES; k++) ej_phase_mark(h, k);
   if (st == EJ_OK) st = ej_finish(h, nullptr);
   if (st != EJ_OK) {
-    index_release(ix);
+    cudaStreamSynchronize(h->stream);
+    index_release(ix, h->stream);
     return st;
   }
   *out = ix;
@@ -79,8 +124,8 @@ extern "C" ej_status ej_sort_index_build(ej_handle* h, const ej_tuple* R, uint64
 extern "C" ej_status ej_index_free(ej_handle* h, ej_index* idx) {
   if (!h || !idx) return EJ_ERR_INVALID;
   EJ_CUDA(h, cudaSetDevice(idx->device));
-  EJ_CUDA(h, cudaStreamSynchronize(h->stream));
-  index_release(idx);
+  EJ_CUDA(h, cudaStreamSynchronize(h->stream));  // no probe of the index is still running on h
+  index_release(idx, h->stream);
   return EJ_OK;
 }
 

@@ -100,7 +100,8 @@ const char* ej_status_name(ej_status s);
 const char* ej_last_error(const ej_handle* h);
 /* bytes of device scratch the handle holds (arena high-water mark) */
 uint64_t ej_scratch_bytes(const ej_handle* h);
-/* release the handle's cached scratch (the next call re-allocates) */
+/* release the handle's cached scratch (the next call re-allocates) and the
+ * memory of the device's index pool that no live index holds */
 ej_status ej_trim(ej_handle* h);
 /* Phase timers, like the reference's (hj.cc:1194-1237) but measured on the
  * device with CUDA events when timing is enabled.  Phases of one join, in
@@ -192,7 +193,9 @@ ej_status ej_distance_join_count(ej_handle* h, uint32_t dims, const void* R, uin
  * ej_index_free.  The reference builds both indexes on the CPU and uploads them:
  * hash index joins/innerJoin_gpu/main_street/inner-idx-bnlj.cc:148-181 (createIndex),
  * sort index joins/innerJoin_gpu/sort_index/main_street/inner-idx-bnlj.cc:175-217
- * (qsort + createIndex).  R must stay valid while the index is used. */
+ * (qsort + createIndex).  R must stay valid while the index is used.  An
+ * index's storage comes from a stream-ordered memory pool of its device that
+ * keeps freed index memory for the next index (ej_trim gives it back). */
 ej_status ej_hash_index_build(ej_handle* h, const ej_tuple* R, uint64_t nR, ej_index** out);
 ej_status ej_sort_index_build(ej_handle* h, const ej_tuple* R, uint64_t nR, ej_index** out);
 ej_status ej_index_free(ej_handle* h, ej_index* idx);
