@@ -226,58 +226,62 @@ extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_
 namespace {
 
 constexpr int ST_THREADS = 256;
+constexpr int ST_WARPS = ST_THREADS / 32;
 constexpr int ST_ITEMS = 4;
-constexpr int ST_TILE = ST_THREADS * ST_ITEMS;
+constexpr int ST_WTILE = 32 * ST_ITEMS;  // fact rows per warp
 
-// rows of fact row f: (matches of F1[f].val in D1) x (matches of F2[f].val in D2)
+// One pass over the fact rows: lane l of a warp takes rows base + 32j + l;
+// the runs of all its F1 vals in D1 are found together, then those of the F2
+// vals of the rows that matched in D2; a row's results are the cross product
+// of its two runs.  Each item j gets a warp scan of its result counts, so the
+// warp's results are ordered item by item and lanes write consecutive rows
+// (one 32-byte row per lane and item when both dimensions have unique keys);
+// the warp reserves its rows with one atomic add on the cursor (rows at or
+// past cap are dropped, the cursor ends at the exact count).
 __global__ void __launch_bounds__(ST_THREADS)
-star_count_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ F2, uint64_t nF, ej_table_view t1,
-                  ej_table_view t2, unsigned long long* __restrict__ tile_count) {
-  __shared__ unsigned long long warp_tmp[ST_THREADS / 32 + 1];
-  const uint64_t base = (uint64_t)blockIdx.x * ST_TILE;
-  unsigned long long c = 0;
-#pragma unroll
-  for (int j = 0; j < ST_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * ST_THREADS + threadIdx.x;
-    if (idx >= nF) continue;
-    uint32_t lo1, c1, lo2, c2 = 0;
-    EjRun<EJ_TABLE_HASH>::find(t1, __ldcs(&F1[idx].val), lo1, c1);
-    if (c1) EjRun<EJ_TABLE_HASH>::find(t2, __ldcs(&F2[idx].val), lo2, c2);
-    c += (unsigned long long)c1 * c2;
-  }
-  unsigned long long total;
-  ej_block_exclusive_sum<ST_THREADS, unsigned long long>(c, warp_tmp, &total);
-  if (threadIdx.x == 0) tile_count[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(ST_THREADS)
-star_write_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ F2, uint64_t nF, ej_table_view t1,
-                  ej_table_view t2, const unsigned long long* __restrict__ tile_off, uint64_t ntiles,
-                  ej_star_result* __restrict__ out, uint64_t cap, ej_dev_status* st) {
-  __shared__ unsigned long long warp_tmp[ST_THREADS / 32 + 1];
-  const uint64_t base = (uint64_t)blockIdx.x * ST_TILE;
+star_fused_kernel(const ej_tuple* __restrict__ F1, const ej_tuple* __restrict__ F2, uint64_t nF, ej_table_view t1,
+                  ej_table_view t2, unsigned long long* __restrict__ cursor, ej_star_result* __restrict__ out,
+                  uint64_t cap, ej_dev_status* st) {
+  const unsigned int lane = threadIdx.x & 31u;
+  const uint64_t base = ((uint64_t)blockIdx.x * ST_WARPS + (threadIdx.x >> 5)) * ST_WTILE;
+  if (base >= nF) return;
   int2 f1[ST_ITEMS], f2[ST_ITEMS];
-  uint32_t lo1[ST_ITEMS], c1[ST_ITEMS], lo2[ST_ITEMS], c2[ST_ITEMS];
-  unsigned long long c = 0;
+  int32_t v1[ST_ITEMS], v2[ST_ITEMS];
+  bool ok1[ST_ITEMS], ok2[ST_ITEMS];
 #pragma unroll
   for (int j = 0; j < ST_ITEMS; j++) {
-    const uint64_t idx = base + (uint64_t)j * ST_THREADS + threadIdx.x;
-    c1[j] = c2[j] = lo1[j] = lo2[j] = 0;
-    f1[j] = f2[j] = make_int2(0, 0);
-    if (idx >= nF) continue;
-    f1[j] = __ldcs(reinterpret_cast<const int2*>(F1) + idx);
-    f2[j] = __ldcs(reinterpret_cast<const int2*>(F2) + idx);
-    EjRun<EJ_TABLE_HASH>::find(t1, f1[j].y, lo1[j], c1[j]);
-    if (c1[j]) EjRun<EJ_TABLE_HASH>::find(t2, f2[j].y, lo2[j], c2[j]);
-    c += (unsigned long long)c1[j] * c2[j];
+    const uint64_t idx = base + (uint64_t)j * 32 + lane;
+    ok1[j] = idx < nF;
+    f1[j] = ok1[j] ? __ldcs(reinterpret_cast<const int2*>(F1) + idx) : make_int2(0, 0);
+    f2[j] = ok1[j] ? __ldcs(reinterpret_cast<const int2*>(F2) + idx) : make_int2(0, 0);
+    v1[j] = f1[j].y;
+    v2[j] = f2[j].y;
   }
-  unsigned long long total;
-  unsigned long long pos = ej_block_exclusive_sum<ST_THREADS, unsigned long long>(c, warp_tmp, &total);
-  pos += tile_off[blockIdx.x];
-  if (blockIdx.x == 0 && threadIdx.x == 0 && tile_off[ntiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  uint32_t lo1[ST_ITEMS], c1[ST_ITEMS], lo2[ST_ITEMS], c2[ST_ITEMS];
+  ej_find_runs<EJ_TABLE_HASH, ST_ITEMS>(t1, v1, ok1, lo1, c1);
+#pragma unroll
+  for (int j = 0; j < ST_ITEMS; j++) ok2[j] = c1[j] != 0;
+  ej_find_runs<EJ_TABLE_HASH, ST_ITEMS>(t2, v2, ok2, lo2, c2);
+  unsigned long long excl[ST_ITEMS], all = 0;
+#pragma unroll
+  for (int j = 0; j < ST_ITEMS; j++) {
+    const unsigned long long n = (unsigned long long)c1[j] * c2[j];
+    const unsigned long long incl = ej_warp_inclusive_sum<unsigned long long>(n);
+    excl[j] = all + incl - n;
+    all += __shfl_sync(EJ_FULL_MASK, incl, 31);
+  }
+  if (all == 0) return;
+  unsigned long long off = 0;
+  if (lane == 0) {
+    off = atomicAdd(cursor, all);
+    if (off + all > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  }
+  off = __shfl_sync(EJ_FULL_MASK, off, 0);
+  if (off >= cap) return;
 #pragma unroll
   for (int j = 0; j < ST_ITEMS; j++) {
     if (!c2[j]) continue;
+    unsigned long long pos = off + excl[j];
     for (uint32_t a = 0; a < c1[j]; a++) {
       const int32_t k1 = __ldg(t1.rkey + lo1[j] + a);
       for (uint32_t b = 0; b < c2[j]; b++) {
@@ -307,10 +311,6 @@ extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tu
   ej_table_plan_t tp1, tp2;
   ej_table_plan(p, tp1, nD1, false, EJ_TABLE_HASH);
   ej_table_plan(p, tp2, nD2, false, EJ_TABLE_HASH);
-  const uint64_t ntiles = (nF + ST_TILE - 1) / ST_TILE;
-  const size_t count_off = p.add((ntiles + 1) * sizeof(unsigned long long));
-  const size_t off_off = p.add((ntiles + 1) * sizeof(unsigned long long));
-  const size_t scan_off = p.add(ej_scan_scratch_bytes(ntiles));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t1, t2;
@@ -320,20 +320,15 @@ extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tu
                         reinterpret_cast<int32_t*>(ej_arena_at(h, tp2.rval_off)), ej_arena_at(h, tp2.aux_off), &t2));
   ej_phase_mark(h, 1);
   ej_phase_mark(h, 2);
-  unsigned long long* tcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, count_off));
-  unsigned long long* toff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, off_off));
-  if (ntiles) {
-    star_count_kernel<<<(unsigned)ntiles, ST_THREADS, 0, h->stream>>>(F1, F2, nF, t1, t2, tcount);
-    EJ_TRY(ej_check_launch(h, "star_count_kernel"));
-  }
-  EJ_TRY(ej_scan_u64_u64(h, tcount, ntiles, toff, ej_arena_at(h, scan_off)));
-  EJ_CUDA(h, cudaMemcpyAsync(h->d_words, toff + ntiles, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
-                             h->stream));
-  ej_phase_mark(h, 3);
-  if (ntiles) {
-    star_write_kernel<<<(unsigned)ntiles, ST_THREADS, 0, h->stream>>>(F1, F2, nF, t1, t2, toff, ntiles, out, out_cap,
+  ej_phase_mark(h, 3);  // one pass: recorded as the write phase
+  EJ_CUDA(h, cudaMemsetAsync(h->d_words, 0, sizeof(unsigned long long), h->stream));  // the row cursor
+  const uint64_t blocks = (nF + (uint64_t)ST_WARPS * ST_WTILE - 1) / ((uint64_t)ST_WARPS * ST_WTILE);
+  if (blocks > 0x7FFFFFFFull) return ej_fail(h, EJ_ERR_INVALID, "star join: %llu fact rows is too many",
+                                             (unsigned long long)nF);
+  if (blocks) {
+    star_fused_kernel<<<(unsigned)blocks, ST_THREADS, 0, h->stream>>>(F1, F2, nF, t1, t2, h->d_words, out, out_cap,
                                                                      h->d_status);
-    EJ_TRY(ej_check_launch(h, "star_write_kernel"));
+    EJ_TRY(ej_check_launch(h, "star_fused_kernel"));
   }
   ej_phase_mark(h, 4);
   uint64_t count = 0;
