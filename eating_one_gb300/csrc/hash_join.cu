@@ -40,8 +40,8 @@
 namespace {
 
 
-// Row bounds of every bucket of the hash-sorted table (tables below
-// EJ_DIR_MIN_ROWS rows): row i (i = nR: the end) begins the buckets between
+// Row bounds of every bucket of the hash-sorted table (tables planned
+// without a key directory): row i (i = nR: the end) begins the buckets between
 // the bucket of row i - 1 and its own; each warp takes 256 consecutive rows.
 __global__ void __launch_bounds__(256)
 bucket_start_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb) {
@@ -57,12 +57,24 @@ __global__ void __launch_bounds__(DIR_THREADS) dir_count_kernel(const int32_t* _
   if (threadIdx.x == 0) tile_keys[blockIdx.x] = total;
 }
 
-// per tile: the largest home_k - k; the header (key count, bits, first hash)
+// per tile: the largest home_k - k; the header (key count, bits, first hash).
+// The directory is kept when the table's runs average two rows or more, or
+// when the caller expects 16 probes per row or more (prefer_dir): there a
+// probe's single slot load repays the build; else the header says bits = 0
+// and the table is probed through bucket bounds (dir_bucket_kernel), whose
+// build is one launch.
 __global__ void __launch_bounds__(DIR_THREADS) dir_tilemax_kernel(const int32_t* __restrict__ rval, uint64_t n,
                                                                   const uint32_t* __restrict__ tile_off,
                                                                   uint32_t ntiles, long long* __restrict__ kmax,
-                                                                  DirHeader* hdr) {
+                                                                  DirHeader* hdr, uint32_t prefer_dir) {
   const unsigned long long nk = tile_off[ntiles];
+  if (!prefer_dir && 2 * nk > n) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      hdr->bits = 0u;
+      hdr->nkeys = nk;
+    }
+    return;
+  }
   const uint32_t bits = dir_bits_for(nk);
   const long long m = dir_tile_max(rval, n, (uint64_t)blockIdx.x * DIR_TILE, tile_off[blockIdx.x], bits, &hdr->hash0);
   if (threadIdx.x == 0) kmax[blockIdx.x] = m;
@@ -74,8 +86,10 @@ __global__ void __launch_bounds__(DIR_THREADS) dir_tilemax_kernel(const int32_t*
 
 // exclusive prefix maximum over the tiles (one block)
 __global__ void __launch_bounds__(1024) dir_prefix_kernel(const long long* __restrict__ kmax, uint32_t ntiles,
-                                                          long long* __restrict__ kpre) {
+                                                          long long* __restrict__ kpre,
+                                                          const DirHeader* __restrict__ hdr) {
   __shared__ long long tmp[1024 / 32];
+  if (hdr->bits == 0) return;  // bucket bounds instead
   const uint64_t per = (ntiles + blockDim.x - 1) / blockDim.x;
   const uint64_t c0 = min((uint64_t)ntiles, threadIdx.x * per), c1 = min((uint64_t)ntiles, c0 + per);
   long long m = LLONG_MIN;
@@ -105,12 +119,23 @@ __global__ void __launch_bounds__(DIR_THREADS) dir_place_kernel(const int32_t* _
                                                                 const uint32_t* __restrict__ tile_off,
                                                                 const long long* __restrict__ kpre, DirHeader* hdr,
                                                                 uint2* __restrict__ dir) {
+  if (hdr->bits == 0) return;  // bucket bounds instead
   dir_tile_place(rval, n, (uint64_t)blockIdx.x * DIR_TILE, tile_off[blockIdx.x], kpre[blockIdx.x], hdr, dir);
 }
 
 __global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restrict__ hdr, uint64_t n,
                                                        uint2* __restrict__ dir) {
+  if (hdr->bits == 0) return;  // bucket bounds instead
   dir_edges(hdr, n, dir, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
+}
+
+// bucket bounds of a table whose header chose them over the directory
+__global__ void __launch_bounds__(256)
+dir_bucket_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb,
+                  const DirHeader* __restrict__ hdr) {
+  if (hdr->bits != 0) return;
+  const uint64_t r0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * 256;
+  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket, EjHashBucketOf{hb});
 }
 
 // the value buckets of a val-sorted table of n rows (2^hb buckets): the
@@ -240,16 +265,20 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta) {
 
 
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
-  if (tp.kind != EJ_TABLE_HASH) return EJ_VBUCKET_HEADER_BYTES + (size_t(1) << tp.hb) * sizeof(uint2);
-  return tp.use_dir ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint2) : (size_t(1) << tp.hb) * sizeof(uint2);
+  const size_t buckets = (size_t(1) << tp.hb) * sizeof(uint2);
+  if (tp.kind != EJ_TABLE_HASH) return EJ_VBUCKET_HEADER_BYTES + buckets;
+  // a directory table keeps room for the bucket bounds its build may choose instead
+  return tp.use_dir ? DIR_HEADER_BYTES + ej_dir_capacity(tp.nR) * sizeof(uint2) + buckets : buckets;
 }
 
 size_t ej_table_col_bytes(uint64_t nR) { return (size_t)(nR + EJ_TABLE_PAD) * sizeof(int32_t); }
 
-void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta) {
+void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta,
+                   uint64_t n_probe) {
   tp.kind = kind;
   tp.nR = nR;
-  tp.use_dir = kind == EJ_TABLE_HASH && nR >= EJ_DIR_MIN_ROWS;
+  tp.prefer_dir = n_probe > 16 * nR;
+  tp.use_dir = kind == EJ_TABLE_HASH && (nR >= EJ_DIR_MIN_ROWS || (tp.prefer_dir && nR >= EJ_DIR_PROBE_MIN_ROWS));
   tp.hb = ej_table_bucket_bits(nR, delta);  // hash buckets, or value buckets of a sorted table
   tp.passes = 4;  // all 32 key bits: equal keys end up adjacent
   if (!own_storage) {
@@ -311,6 +340,7 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
   } else if (tp.kind == EJ_TABLE_HASH) {
     DirHeader* hdr = static_cast<DirHeader*>(aux);
     uint2* dir = reinterpret_cast<uint2*>(static_cast<char*>(aux) + DIR_HEADER_BYTES);
+    uint2* bucket = dir + ej_dir_capacity(tp.nR);
     const uint32_t tiles = (uint32_t)((tp.nR + DIR_TILE - 1) / DIR_TILE);
     uint32_t* keys = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.dir_keys_off));
     uint32_t* off = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.dir_off_off));
@@ -320,12 +350,15 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
       dir_count_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, keys);
       EJ_TRY(ej_check_launch(h, "dir_count_kernel"));
       EJ_TRY(ej_scan_u32_u32(h, keys, tiles, off, ej_arena_at(h, tp.dir_scan_off)));
-      dir_tilemax_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, tiles, kmax, hdr);
+      dir_tilemax_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, tiles, kmax, hdr, tp.prefer_dir ? 1u : 0u);
       EJ_TRY(ej_check_launch(h, "dir_tilemax_kernel"));
-      dir_prefix_kernel<<<1, 1024, 0, h->stream>>>(kmax, tiles, kpre);
+      dir_prefix_kernel<<<1, 1024, 0, h->stream>>>(kmax, tiles, kpre, hdr);
       EJ_TRY(ej_check_launch(h, "dir_prefix_kernel"));
       dir_place_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, kpre, hdr, dir);
       EJ_TRY(ej_check_launch(h, "dir_place_kernel"));
+      const uint64_t bblocks = (tp.nR + 1 + 2047) / 2048;  // 256 rows per warp, 8 warps per block
+      dir_bucket_kernel<<<(unsigned)bblocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb, hdr);
+      EJ_TRY(ej_check_launch(h, "dir_bucket_kernel"));
     } else {  // no rows: no keys, two home slots
       const DirHeader empty = {1u, 0u, 0ull, 0ull, 0ull};
       EJ_CUDA(h, cudaMemcpyAsync(hdr, &empty, sizeof empty, cudaMemcpyHostToDevice, h->stream));
@@ -334,6 +367,7 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
     EJ_TRY(ej_check_launch(h, "dir_edge_kernel"));
     view->dir = dir;
     view->dir_bits = &hdr->bits;
+    view->bucket = bucket;
   } else {  // sorted: value buckets, header first
     EjValueBuckets* vh = static_cast<EjValueBuckets*>(aux);
     uint2* bucket = reinterpret_cast<uint2*>(static_cast<char*>(aux) + EJ_VBUCKET_HEADER_BYTES);
@@ -479,7 +513,7 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   const uint32_t pb = (mode == 1) ? 0u : ej_probe_partition_bits(h, nR, nS);
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR));
+  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR), nS);
   ej_probe_layout L;
   // the build-side-only join keeps its rows in probe order (the batched joins
   // give the same rows in the same order); the others take the one-pass probe

@@ -7,16 +7,23 @@
 
 #include "ej_internal.h"
 
-// Hash tables of at least this many rows carry a key directory (one load per
-// probe, seven build launches); smaller ones carry bucket bounds (one build
-// launch; the bucket scan costs nothing extra while the table sits in L2)
-constexpr uint64_t EJ_DIR_MIN_ROWS = 1ull << 20;
+// Hash tables of at least EJ_DIR_MIN_ROWS rows may carry a key directory (one
+// load per probe, seven build launches): the build keeps it when the table's
+// runs average two rows or more and otherwise switches to bucket bounds (one
+// build launch); tables from EJ_DIR_PROBE_MIN_ROWS rows keep it whenever the
+// caller probes 16 rows per table row or more.  Smaller tables carry bucket
+// bounds (the bucket scan costs no more than a directory lookup while the
+// table sits in L2).
+constexpr uint64_t EJ_DIR_MIN_ROWS = 1ull << 22;
+constexpr uint64_t EJ_DIR_PROBE_MIN_ROWS = 1ull << 20;
 // a sorted table's aux storage: the value buckets' header, then the bounds
 constexpr size_t EJ_VBUCKET_HEADER_BYTES = 256;
 
 struct ej_table_plan_t {
   int kind = EJ_TABLE_HASH;
-  bool use_dir = false;  // hash tables: key directory (else bucket bounds)
+  bool use_dir = false;     // hash tables: key directory (else bucket bounds), unless the build
+                            // finds short runs and no probe-heavy caller (then bucket bounds too)
+  bool prefer_dir = false;  // the caller probes 16 or more rows per table row: keep the directory
   uint64_t nR = 0;
   uint32_t hb = 1;      // bucket bits (hash buckets, or value buckets of a sorted table)
   uint32_t passes = 4;  // LSD radix passes over the 32-bit key
@@ -49,7 +56,9 @@ size_t ej_table_col_bytes(uint64_t nR);
 // bytes of the bucket bounds or the key directory (hash), or the value
 // buckets and their header (sorted)
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp);
-void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta = 0);
+// n_probe: the probe rows the caller expects (0: unknown)
+void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta = 0,
+                   uint64_t n_probe = 0);
 ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, int32_t* rkey, int32_t* rval,
                          void* aux, ej_table_view* view);
 

@@ -205,7 +205,7 @@ extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_
   const uint32_t pb = ej_probe_partition_bits(h, nR, nS);
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR));
+  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR), nS);
   ej_probe_layout L;
   ej_probe_layout_add(p, L, nS, pb, /*count_only=*/false);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
@@ -309,8 +309,8 @@ extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tu
   EJ_TRY(ej_check_out(h, out, out_cap, out_count));
   ej_plan_bytes p;
   ej_table_plan_t tp1, tp2;
-  ej_table_plan(p, tp1, nD1, false, EJ_TABLE_HASH);
-  ej_table_plan(p, tp2, nD2, false, EJ_TABLE_HASH);
+  ej_table_plan(p, tp1, nD1, false, EJ_TABLE_HASH, 0, nF);
+  ej_table_plan(p, tp2, nD2, false, EJ_TABLE_HASH, 0, nF);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t1, t2;

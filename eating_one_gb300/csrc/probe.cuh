@@ -2,14 +2,16 @@
 //
 // A table stores R as rkey[]/rval[] in one order (ej_table_view).  In both
 // kinds the matches of a value v form one contiguous run [lo, lo + c):
-//   EJ_TABLE_HASH    rows sorted by hash32(val).  Single tables of 2^20 rows
-//                    or more carry a key directory (8-byte entries {hash,
-//                    lo} in hash order, linear probing from slot hash >>
-//                    (32 - bits), each slot holding the first key at or after
-//                    it, so c is the next slot's start minus lo); smaller and
-//                    batched tables carry bucket bounds: the run lies inside
-//                    bucket b = top hb hash bits, rows [bucket[b].x,
-//                    bucket[b].y) (one 8-byte load);
+//   EJ_TABLE_HASH    rows sorted by hash32(val).  Single tables of 2^22 rows
+//                    or more whose runs average two rows or more, and those
+//                    of 2^20 rows or more whose caller probes 16 rows per
+//                    table row, carry a key directory (8-byte entries {hash, lo} in hash order,
+//                    linear probing from slot hash >> (32 - bits), each slot
+//                    holding the first key at or after it, so c is the next
+//                    slot's start minus lo); the others, smaller and batched
+//                    tables carry bucket bounds: the run lies inside bucket b
+//                    = top hb hash bits, rows [bucket[b].x, bucket[b].y) (one
+//                    8-byte load);
 //   EJ_TABLE_SORTED  rows sorted by val, with bucket bounds over value
 //                    prefixes: bucket b = (v - vmin) >> vshift (the table's
 //                    smallest and largest vals and the shift in a small
@@ -275,11 +277,13 @@ __device__ __forceinline__ void ej_find_runs_bucket(const ej_table_view& t, cons
 template <int N>
 __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const int32_t (&v)[N], const bool (&ok)[N],
                                                   uint32_t (&lo)[N], uint32_t (&c)[N]) {
-  if (t.dir) {
+  // a directory table whose build chose bucket bounds has bits = 0
+  const uint32_t bits = t.dir ? __ldg(t.dir_bits) : 0u;
+  if (bits) {
     // key directory: every slot holds the first key at or after it; walk past
     // smaller hashes, then the run ends at the first slot with another start
     // (slot + 1 never passes the sentinels after the last entry)
-    const uint32_t shift = 32u - __ldg(t.dir_bits);
+    const uint32_t shift = 32u - bits;
     uint32_t hv[N], slot[N];
     uint2 a[N], b[N];
 #pragma unroll

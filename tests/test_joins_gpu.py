@@ -169,6 +169,24 @@ def test_capacity_and_guard(engine):
     assert engine.count("hash", dev(R), dev(S)) == total
 
 
+@pytest.mark.parametrize("n,dup,s_rows", [(1 << 22, 1, 1 << 23), (1 << 22, 3, 1 << 23), (1 << 20, 1, 17 << 20)])
+def test_directory_or_buckets(engine, n, dup, s_rows):
+    """A 2^22-row table keeps its key directory when its runs average two rows
+    or more (else its build switches to bucket bounds); a 2^20-row table has
+    one when the probe side is 16 times its size or more.  Every case must give
+    the oracle's rows."""
+    rng = np.random.default_rng(40 + dup)
+    keys = rng.choice(1 << 24, size=n // dup + 1, replace=False).astype(np.int32)
+    R = np.stack([np.arange(n, dtype=np.int32), np.repeat(keys, dup)[:n]], axis=1)
+    R = R[rng.permutation(n)]
+    S = rel(rng, s_rows, 0, 1 << 24, key_base=n)
+    S[: s_rows // 2, 1] = keys[rng.integers(0, len(keys), s_rows // 2)]
+    same_multiset(engine.join("hash", dev(R), dev(S)), O.hash_join(R, S))
+    if s_rows < (4 << 20):
+        same_multiset(engine.join("left_outer", dev(R), dev(S)), O.left_outer_join(R, S))
+        same_multiset(engine.join("hash_index", dev(R), dev(S)), O.hash_index_join(R, S))
+
+
 def test_wide_buckets(engine):
     """Two outliers stretch the value range, so a sorted index's value buckets
     hold tens of thousands of distinct vals (runs found by binary search past
