@@ -5,10 +5,10 @@
 // For a stream of joins of uneven sizes (most of them small) that is launch-
 // and latency-bound.  Here a batch of joins is one fixed sequence of launches,
 // whatever the number of joins in it:
-//   gather      every R into one concatenated array (one launch over R tiles)
 //   build       four segmented LSD radix passes: tiles never cross a join and
 //               the digit histograms are laid out join by join, so one scan
-//               places every join's rows in its own range, hash-sorted
+//               places every join's rows in its own range, hash-sorted (the
+//               first pass reads every join's R where it lies)
 //   starts      every join's bucket starts in one launch (its own bucket bits;
 //               a batch's tables are small enough for L2, where the bucket
 //               scan is as fast as a key directory and one launch builds it)
@@ -44,15 +44,6 @@ struct BatchJoin {
 struct BatchPTile {
   uint32_t join, local;
 };
-
-__global__ void batch_gather_kernel(const ej_rx_tile* __restrict__ tiles, const BatchJoin* __restrict__ joins,
-                                    ej_tuple* __restrict__ rcat) {
-  const ej_rx_tile d = tiles[blockIdx.x];
-  const BatchJoin& j = joins[d.pad];
-  const uint2* src = reinterpret_cast<const uint2*>(j.R) + (d.start - j.r_row0);
-  uint2* dst = reinterpret_cast<uint2*>(rcat) + d.start;
-  for (uint32_t i = threadIdx.x; i < d.n; i += blockDim.x) dst[i] = __ldcs(src + i);
-}
 
 // bucket bounds of every join: the block of one R tile fills the gaps
 // between the buckets of consecutive rows of its join; the join's last row
@@ -133,6 +124,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
       d.cell0 = (uint32_t)(cells + t);
       d.stride = rt;
       d.pad = i;
+      d.src = nullptr;
       rtiles.push_back(d);
     }
     cells += (uint64_t)rt * 256;
@@ -150,9 +142,9 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   ej_plan_bytes p;
   const size_t joins_off = p.add(n * sizeof(BatchJoin));
   const size_t rtiles_off = p.add(std::max<size_t>(rtiles.size(), 1) * sizeof(ej_rx_tile));
+  const size_t rtiles0_off = p.add(std::max<size_t>(rtiles.size(), 1) * sizeof(ej_rx_tile));
   const size_t ptiles_off = p.add(std::max<size_t>(ptiles.size(), 1) * sizeof(BatchPTile));
   const size_t sbase_off = p.add(n * sizeof(unsigned long long));
-  const size_t rcat_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
   const size_t tmpa_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
   const size_t tmpb_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
   const size_t rkey_off = p.add(ej_table_col_bytes(nr_total));
@@ -182,6 +174,10 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
                pb = ptiles.size() * sizeof(BatchPTile), sb = n * sizeof(unsigned long long);
   EJ_CUDA(h, cudaMemcpyAsync(A + joins_off, joins.data(), jb, cudaMemcpyHostToDevice, h->stream));
   if (rb) EJ_CUDA(h, cudaMemcpyAsync(A + rtiles_off, rtiles.data(), rb, cudaMemcpyHostToDevice, h->stream));
+  // the first radix pass reads every join's R where it lies: the same tiles
+  // with their source rows
+  for (ej_rx_tile& d : rtiles) d.src = joins[d.pad].R + (d.start - joins[d.pad].r_row0);
+  if (rb) EJ_CUDA(h, cudaMemcpyAsync(A + rtiles0_off, rtiles.data(), rb, cudaMemcpyHostToDevice, h->stream));
   if (pb) EJ_CUDA(h, cudaMemcpyAsync(A + ptiles_off, ptiles.data(), pb, cudaMemcpyHostToDevice, h->stream));
   EJ_CUDA(h, cudaMemcpyAsync(A + sbase_off, sbase.data(), sb, cudaMemcpyHostToDevice, h->stream));
   EJ_CUDA(h, cudaMemsetAsync(d_counts, 0, n * sizeof(unsigned long long), h->stream));
@@ -191,19 +187,15 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
 
   ej_phase_begin(h);
   if (!rtiles.empty()) {
-    ej_tuple* rcat = reinterpret_cast<ej_tuple*>(A + rcat_off);
-    batch_gather_kernel<<<(unsigned)rtiles.size(), 256, 0, h->stream>>>(drt, djoins, rcat);
-    EJ_TRY(ej_check_launch(h, "batch_gather_kernel"));
     ej_tuple* tmp[2] = {reinterpret_cast<ej_tuple*>(A + tmpa_off), reinterpret_cast<ej_tuple*>(A + tmpb_off)};
-    const ej_tuple* src = rcat;
-    for (uint32_t pass = 0; pass < 4; pass++) {
-      if (pass == 3) {
-        EJ_TRY(ej_radix_pass_soa(h, rp, src, rkey, rval, 24u, 8u, EJ_DIGIT_HASH));
-      } else {
-        EJ_TRY(ej_radix_pass(h, rp, src, tmp[pass & 1], 8u * pass, 8u, EJ_DIGIT_HASH));
-        src = tmp[pass & 1];
-      }
-    }
+    ej_radix_plan rp0 = rp;
+    rp0.tiles = reinterpret_cast<const ej_rx_tile*>(A + rtiles0_off);
+    // pass 0 reads the joins' R arrays in place; its order within a digit is
+    // never used (unordered ranking)
+    EJ_TRY(ej_partition_pass_src(h, rp0, tmp[0], 0u, 8u));
+    EJ_TRY(ej_radix_pass(h, rp, tmp[0], tmp[1], 8u, 8u, EJ_DIGIT_HASH));
+    EJ_TRY(ej_radix_pass(h, rp, tmp[1], tmp[0], 16u, 8u, EJ_DIGIT_HASH));
+    EJ_TRY(ej_radix_pass_soa(h, rp, tmp[0], rkey, rval, 24u, 8u, EJ_DIGIT_HASH));
   }
   // joins with an empty R keep all-zero bucket starts
   EJ_CUDA(h, cudaMemsetAsync(bucket, 0, start_total * sizeof(uint2), h->stream));

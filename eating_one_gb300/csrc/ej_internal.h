@@ -133,6 +133,7 @@ constexpr uint32_t EJ_RX_TILE = 4096;  // rows per radix tile
 struct ej_rx_tile {
   unsigned long long start;
   uint32_t n, cell0, stride, pad;
+  const ej_tuple* src;  // the tile's first input row (ej_partition_pass_src; other passes: input + start)
 };
 
 struct ej_radix_plan {
@@ -153,6 +154,10 @@ ej_status ej_partition_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tupl
                             uint32_t shift, uint32_t bits, int digit_kind = EJ_DIGIT_HASH);
 ej_status ej_radix_pass_soa(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, int32_t* out_keys,
                             int32_t* out_vals, uint32_t shift, uint32_t bits, int digit_kind);
+// the unordered pass by hash digits over tiles whose descriptors carry their
+// source rows (src), which may lie in separate arrays
+ej_status ej_partition_pass_src(ej_handle* h, const ej_radix_plan& rp, ej_tuple* out, uint32_t shift,
+                                uint32_t bits);
 
 // ---- probe targets (hash_join.cu) -----------------------------------------
 // R is stored as two arrays, rkey[] and rval[], in one order:

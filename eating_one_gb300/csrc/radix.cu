@@ -37,28 +37,33 @@ __device__ __forceinline__ uint32_t rx_digit(int32_t val, uint32_t shift, uint32
 // nullptr; histogram cell of digit d = d * ntiles + tile), or one entry of a
 // descriptor array whose tiles never cross a segment (batched joins).
 struct RxTile {
-  uint64_t start;
+  const ej_tuple* base;  // the tile's first input row
   uint32_t n, cell0, stride;
 };
 
-__device__ __forceinline__ RxTile rx_tile(const ej_rx_tile* tiles, uint64_t n, uint32_t ntiles) {
+// SRC: the descriptors carry their tiles' source rows (a pass over inputs
+// that lie in separate arrays)
+template <bool SRC>
+__device__ __forceinline__ RxTile rx_tile(const ej_tuple* in, const ej_rx_tile* tiles, uint64_t n,
+                                          uint32_t ntiles) {
   RxTile t;
   if (tiles) {
-    const ej_rx_tile d = tiles[blockIdx.x];
-    t.start = d.start;
+    const ej_rx_tile& d = tiles[blockIdx.x];
+    t.base = SRC ? d.src : in + d.start;
     t.n = d.n;
     t.cell0 = d.cell0;
     t.stride = d.stride;
   } else {
-    t.start = (uint64_t)blockIdx.x * RX_TILE;
-    t.n = (uint32_t)min((uint64_t)RX_TILE, n - t.start);
+    const uint64_t start = (uint64_t)blockIdx.x * RX_TILE;
+    t.base = in + start;
+    t.n = (uint32_t)min((uint64_t)RX_TILE, n - start);
     t.cell0 = blockIdx.x;
     t.stride = ntiles;
   }
   return t;
 }
 
-template <int KIND>
+template <int KIND, bool SRC = false>
 __global__ void __launch_bounds__(RX_THREADS)
 rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __restrict__ tiles,
                uint32_t* __restrict__ hist, uint32_t ntiles, uint32_t shift, uint32_t mask) {
@@ -66,23 +71,22 @@ rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __
   const uint32_t ndig = mask + 1u;
   for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&cnt[0][0])[i] = 0u;
   __syncthreads();
-  const RxTile tl = rx_tile(tiles, n, ntiles);
-  n = tl.start + tl.n;  // rows of this tile end here
+  const RxTile tl = rx_tile<SRC>(in, tiles, n, ntiles);
   const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint64_t wbase = tl.start + (uint64_t)warp * RX_WARP_SPAN;
-  const int* vals = reinterpret_cast<const int*>(in) + 1;  // .val of tuple i at vals[2*i]
+  const uint32_t wbase = warp * RX_WARP_SPAN;
+  const int* vals = reinterpret_cast<const int*>(tl.base) + 1;  // .val of the tile's tuple i at vals[2*i]
   int v[RX_ROUNDS];
 #pragma unroll
   for (int r = 0; r < RX_ROUNDS; r++) {
-    const uint64_t idx = wbase + (uint64_t)r * 32u + lane;
-    v[r] = idx < n ? __ldcs(vals + 2 * idx) : 0;
+    const uint32_t i = wbase + r * 32u + lane;
+    v[r] = i < tl.n ? __ldcs(vals + 2 * (uint64_t)i) : 0;
   }
   // warp-private histograms: counting order does not matter, so plain
   // shared-memory atomics (same-digit lanes of one instruction serialise in hardware)
 #pragma unroll
   for (int r = 0; r < RX_ROUNDS; r++) {
-    const uint64_t idx = wbase + (uint64_t)r * 32u + lane;
-    if (idx < n) atomicAdd(&cnt[warp][rx_digit<KIND>(v[r], shift, mask)], 1u);
+    const uint32_t i = wbase + r * 32u + lane;
+    if (i < tl.n) atomicAdd(&cnt[warp][rx_digit<KIND>(v[r], shift, mask)], 1u);
   }
   __syncthreads();
   for (uint32_t d = threadIdx.x; d < ndig; d += RX_THREADS) {
@@ -106,7 +110,7 @@ struct RxScatterSmem {
 // digit's run is left to shared-memory atomics (a one-pass partition, where no
 // later pass depends on it), which takes about a fifth of the ranking's
 // instructions
-template <int KIND, bool SOA, bool STABLE>
+template <int KIND, bool SOA, bool STABLE, bool SRC = false>
 __global__ void __launch_bounds__(RX_THREADS, 4)
 rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __restrict__ tiles,
                   ej_tuple* __restrict__ out, int32_t* __restrict__ out_keys, int32_t* __restrict__ out_vals,
@@ -115,14 +119,14 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile*
   RxScatterSmem& sm = *reinterpret_cast<RxScatterSmem*>(rx_smem_raw);
   const uint32_t ndig = mask + 1u;
   const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const RxTile tl = rx_tile(tiles, n, ntiles);
+  const RxTile tl = rx_tile<SRC>(in, tiles, n, ntiles);
   const uint32_t tile_n = tl.n;
   for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&sm.cnt[0][0])[i] = 0u;
 
   // 1. the warp's RX_ROUNDS x 32 consecutive tuples into registers (coalesced,
   //    streaming: read once)
   const uint32_t wbase = warp * RX_WARP_SPAN;
-  const uint2* src = reinterpret_cast<const uint2*>(in + tl.start);
+  const uint2* src = reinterpret_cast<const uint2*>(tl.base);
   uint2 tup[RX_ROUNDS];
 #pragma unroll
   for (int r = 0; r < RX_ROUNDS; r++) {
@@ -219,7 +223,7 @@ void ej_radix_plan_add(ej_plan_bytes& p, ej_radix_plan& rp, uint64_t n) {
   rp.scan_off = p.add(ej_scan_scratch_bytes(cells));
 }
 
-template <int KIND, bool SOA, bool STABLE = true>
+template <int KIND, bool SOA, bool STABLE = true, bool SRC = false>
 static ej_status radix_pass_kind(ej_handle* h, const ej_radix_plan& rp, const ej_tuple* in, ej_tuple* out,
                                  int32_t* out_keys, int32_t* out_vals, uint32_t shift, uint32_t bits) {
   const uint32_t mask = (1u << bits) - 1u;
@@ -229,12 +233,13 @@ static ej_status radix_pass_kind(ej_handle* h, const ej_radix_plan& rp, const ej
   uint32_t* hist = reinterpret_cast<uint32_t*>(ej_arena_at(h, rp.hist_off));
   uint32_t* offs = reinterpret_cast<uint32_t*>(ej_arena_at(h, rp.offs_off));
   if (rp.tiles && bits != 8) return ej_fail(h, EJ_ERR_INTERNAL, "segmented radix passes use 8-bit digits");
-  rx_hist_kernel<KIND><<<rp.ntiles, RX_THREADS, 0, h->stream>>>(in, rp.n, rp.tiles, hist, rp.ntiles, shift, mask);
+  rx_hist_kernel<KIND, SRC><<<rp.ntiles, RX_THREADS, 0, h->stream>>>(in, rp.n, rp.tiles, hist, rp.ntiles, shift,
+                                                                     mask);
   EJ_TRY(ej_check_launch(h, "rx_hist_kernel"));
   EJ_TRY(ej_scan_u32_u32(h, hist, cells, offs, ej_arena_at(h, rp.scan_off)));
-  EJ_CUDA(h, cudaFuncSetAttribute(rx_scatter_kernel<KIND, SOA, STABLE>,
+  EJ_CUDA(h, cudaFuncSetAttribute(rx_scatter_kernel<KIND, SOA, STABLE, SRC>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RxScatterSmem)));
-  rx_scatter_kernel<KIND, SOA, STABLE><<<rp.ntiles, RX_THREADS, sizeof(RxScatterSmem), h->stream>>>(
+  rx_scatter_kernel<KIND, SOA, STABLE, SRC><<<rp.ntiles, RX_THREADS, sizeof(RxScatterSmem), h->stream>>>(
       in, rp.n, rp.tiles, out, out_keys, out_vals, offs, rp.ntiles, shift, mask);
   return ej_check_launch(h, "rx_scatter_kernel");
 }
@@ -270,4 +275,12 @@ ej_status ej_partition_pass(ej_handle* h, const ej_radix_plan& rp, const ej_tupl
   if (digit_kind == EJ_DIGIT_VALUE)
     return radix_pass_kind<EJ_DIGIT_VALUE, false, false>(h, rp, in, out, nullptr, nullptr, shift, bits);
   return radix_pass_kind<EJ_DIGIT_HASH, false, false>(h, rp, in, out, nullptr, nullptr, shift, bits);
+}
+
+ej_status ej_partition_pass_src(ej_handle* h, const ej_radix_plan& rp, ej_tuple* out, uint32_t shift,
+                                uint32_t bits) {
+  if (rp.n == 0) return EJ_OK;
+  EJ_TRY(check_digit(h, shift, bits));
+  if (!rp.tiles) return ej_fail(h, EJ_ERR_INTERNAL, "a pass over separate inputs needs tile descriptors");
+  return radix_pass_kind<EJ_DIGIT_HASH, false, false, true>(h, rp, nullptr, out, nullptr, nullptr, shift, bits);
 }
