@@ -99,7 +99,6 @@ rx_hist_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile* __
 
 struct RxScatterSmem {
   ej_tuple sorted[RX_TILE];                // 32 KB: the tile in digit order
-  uint8_t sdig[RX_TILE];                   // digit of each sorted position
   uint32_t cnt[RX_WARPS][RX_MAX_DIGITS];   // per-warp digit counters, then bases
   uint32_t gbase[RX_MAX_DIGITS];
   uint32_t warp_tmp[RX_WARPS + 1];
@@ -122,6 +121,11 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile*
   const RxTile tl = rx_tile<SRC>(in, tiles, n, ntiles);
   const uint32_t tile_n = tl.n;
   for (int i = threadIdx.x; i < RX_WARPS * RX_MAX_DIGITS; i += RX_THREADS) (&sm.cnt[0][0])[i] = 0u;
+  // unordered passes: the digit's global offset (thread d) is loaded now, so
+  // that it is in hand when the ranking is done (the stable ranking has no
+  // register to spare for it and loads it afterwards)
+  uint32_t goff = 0;
+  if (!STABLE && threadIdx.x < ndig) goff = offs[tl.cell0 + (uint64_t)threadIdx.x * tl.stride];
 
   // 1. the warp's RX_ROUNDS x 32 consecutive tuples into registers (coalesced,
   //    streaming: read once)
@@ -181,7 +185,8 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile*
     const uint32_t d = threadIdx.x;
 #pragma unroll
     for (int w = 0; w < RX_WARPS; w++) sm.cnt[w][d] += dstart;
-    sm.gbase[d] = offs[tl.cell0 + (uint64_t)d * tl.stride] - dstart;
+    if (STABLE) goff = offs[tl.cell0 + (uint64_t)d * tl.stride];
+    sm.gbase[d] = goff - dstart;
   }
   __syncthreads();
 
@@ -192,7 +197,6 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile*
       const uint32_t d = packed[r] >> 16;
       const uint32_t pos = sm.cnt[warp][d] + (packed[r] & 0xFFFFu);
       reinterpret_cast<uint2*>(sm.sorted)[pos] = tup[r];
-      sm.sdig[pos] = (uint8_t)d;
     }
   }
   __syncthreads();
@@ -200,7 +204,7 @@ rx_scatter_kernel(const ej_tuple* __restrict__ in, uint64_t n, const ej_rx_tile*
   // 5. write digit runs: sorted position k goes to gbase[digit] + k
   for (uint32_t k = threadIdx.x; k < tile_n; k += RX_THREADS) {
     const uint2 t = reinterpret_cast<const uint2*>(sm.sorted)[k];
-    const uint32_t pos = sm.gbase[sm.sdig[k]] + k;
+    const uint32_t pos = sm.gbase[rx_digit<KIND>((int32_t)t.y, shift, mask)] + k;
     if (SOA) {
       out_keys[pos] = (int32_t)t.x;
       out_vals[pos] = (int32_t)t.y;
