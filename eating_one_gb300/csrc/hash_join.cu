@@ -129,13 +129,16 @@ __global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restri
   dir_edges(hdr, n, dir, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
 }
 
-// bucket bounds of a table whose header chose them over the directory
+// bucket bounds of a table whose header chose them over the directory; a
+// few blocks per SM stride over the rows, so that the launch costs next to
+// nothing when the directory stays
 __global__ void __launch_bounds__(256)
 dir_bucket_kernel(const int32_t* __restrict__ rval, uint64_t nR, uint2* __restrict__ bucket, uint32_t hb,
                   const DirHeader* __restrict__ hdr) {
   if (hdr->bits != 0) return;
-  const uint64_t r0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * 256;
-  if (r0 <= nR) ej_bucket_bounds_warp(rval, nR, r0, hb, bucket, EjHashBucketOf{hb});
+  const uint64_t warps = (uint64_t)gridDim.x * 8;
+  for (uint64_t w = (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5); w * 256 <= nR; w += warps)
+    ej_bucket_bounds_warp(rval, nR, w * 256, hb, bucket, EjHashBucketOf{hb});
 }
 
 // the value buckets of a val-sorted table of n rows (2^hb buckets): the
@@ -356,7 +359,7 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
       EJ_TRY(ej_check_launch(h, "dir_prefix_kernel"));
       dir_place_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, kpre, hdr, dir);
       EJ_TRY(ej_check_launch(h, "dir_place_kernel"));
-      const uint64_t bblocks = (tp.nR + 1 + 2047) / 2048;  // 256 rows per warp, 8 warps per block
+      const uint64_t bblocks = std::min<uint64_t>((tp.nR + 1 + 2047) / 2048, (uint64_t)h->num_sms * 8);
       dir_bucket_kernel<<<(unsigned)bblocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb, hdr);
       EJ_TRY(ej_check_launch(h, "dir_bucket_kernel"));
     } else {  // no rows: no keys, two home slots
