@@ -278,7 +278,8 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
     d2 / d3: `repeat` distance joins of 2^(19 - scale) x 2^(19 - scale) points
     (after one count-only call); c5_batch: `repeat` batches of the served
     stream's 256 request instances; c4_index: `repeat` times a hash index and a
-    sort index built on C4's R and probed with its S."""
+    sort index built on C4's R and probed with its S; c4_star: `repeat` star
+    joins."""
     import torch
 
     from eating_one_gb300.build import build
@@ -300,6 +301,15 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
         got = d_counts.cpu().tolist()
         assert got == pool.expected
         print(json.dumps({"profile_case": name, "joins": len(got), "rows": int(sum(got))}), flush=True)
+        return
+    if name == "c4_star":  # `repeat` 3-way star joins of C4's fact and dimension tables
+        w = workload("c4_star", scale)
+        t = {k: eng.generate(v) for k, v in w.items()}
+        out = None
+        for _ in range(repeat):
+            out = eng.star_join3(t["F1"], t["F2"], t["D1"], t["D2"], out=out)
+        print(json.dumps({"profile_case": name, "scale": scale, "F": int(t["F1"].shape[0]),
+                          "rows": int(out.shape[0])}), flush=True)
         return
     if name == "c4_index":  # per repeat: a hash index and a sort index built on C4's R, each probed once
         w = workload("c4", scale)
