@@ -227,11 +227,12 @@ namespace {
 
 constexpr int ST_THREADS = 256;
 constexpr int ST_WARPS = ST_THREADS / 32;
-constexpr int ST_ITEMS = 4;
+constexpr int ST_ITEMS = 2;  // 40 registers, six blocks per SM (four items: 74, three blocks, 4% slower)
 constexpr int ST_WTILE = 32 * ST_ITEMS;  // fact rows per warp
 
-// One pass over the fact rows: lane l of a warp takes rows base + 32j + l;
-// the runs of all its F1 vals in D1 are found together, then those of the F2
+// One pass over the fact rows: lane l of a warp takes rows base + 32j + l
+// (j < ST_ITEMS); the runs of all its F1 vals in D1 are found together, then
+// those of the F2
 // vals of the rows that matched in D2; a row's results are the cross product
 // of its two runs.  Each item j gets a warp scan of its result counts, so the
 // warp's results are ordered item by item and lanes write consecutive rows
