@@ -126,9 +126,6 @@ __device__ __forceinline__ void ej_search_rows(const int32_t* __restrict__ rv, u
   }
 }
 
-template <int KIND>
-struct EjRun;
-
 constexpr int EJ_SCAN_ROUNDS = 2;  // linear rounds of 4 values past a bucket's first 8
 
 // Runs of N probe values at once through bucket bounds (hash tables without
@@ -336,18 +333,6 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
   }
   ej_find_runs_bucket<0, N>(t, v, ok, lo, c);
 }
-
-template <>
-struct EjRun<EJ_TABLE_HASH> {
-  static __device__ __forceinline__ void find(const ej_table_view& t, int32_t v, uint32_t& lo, uint32_t& c) {
-    const int32_t vv[1] = {v};
-    const bool ok[1] = {true};
-    uint32_t l[1], n[1];
-    ej_find_runs_hash<1>(t, vv, ok, l, n);
-    lo = l[0];
-    c = n[0];
-  }
-};
 
 // runs of N probe values (ok[j] false: c[j] = 0)
 template <int KIND, int N>
