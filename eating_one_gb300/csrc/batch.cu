@@ -82,7 +82,7 @@ batch_fused_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __rest
   const unsigned long long total = ej_warp_sum<unsigned long long>(mine);
   if (total == 0) return;
   int32_t kk[PR_ITEMS][PW_PREFETCH];
-  ej_probe_prefetch(j.view, pw, kk);
+  ej_probe_prefetch<EJ_KEYS_CHUNKS>(j.view, pw, kk);
   unsigned long long off = 0;
   if (lane == 0) {
     off = atomicAdd(j.d_count, total);

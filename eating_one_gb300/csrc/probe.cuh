@@ -289,13 +289,15 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
       slot[j] = hv[j] >> shift;
       a[j] = b[j] = make_uint2(0u, 0u);
       if (ok[j]) {
-        // the 16-byte aligned slot pair holding the home slot (the directory
-        // starts 16-byte aligned): both slots needed when it is even
-        const uint4 q = __ldg(reinterpret_cast<const uint4*>(t.dir) + (slot[j] >> 1));
+        // the home slot and the next: one 16-byte load of the aligned pair
+        // when the home slot is even (the directory starts 16-byte aligned),
+        // else two 8-byte loads (the L1 data path pays for the bytes it
+        // delivers, and the pair holding an odd slot brings one not needed)
         if (slot[j] & 1u) {
-          a[j] = make_uint2(q.z, q.w);
+          a[j] = __ldg(t.dir + slot[j]);
           b[j] = __ldg(t.dir + slot[j] + 1);
         } else {
+          const uint4 q = __ldg(reinterpret_cast<const uint4*>(t.dir) + (slot[j] >> 1));
           a[j] = make_uint2(q.x, q.y);
           b[j] = make_uint2(q.z, q.w);
         }

@@ -91,13 +91,23 @@ __device__ __forceinline__ unsigned long long ej_group_rows(uint32_t c, uint32_t
   return __shfl_sync(EJ_FULL_MASK, incl, 31);
 }
 
-// keys of the first PW_PREFETCH rows of every run: the aligned 8-key window
-// holding them, in one or two 16-byte loads (rkey - voff is 16-byte aligned
-// and the column is padded, so the window stays inside it)
+// keys of the first PW_PREFETCH rows of every run (rkey - voff is 16-byte
+// aligned and the column is padded, so every load stays inside it), in one
+// of two schemes fixed at compile time (the L1 data path pays for the bytes
+// it delivers; both schemes in one kernel cost more than either saves):
+//   EJ_KEYS_WINDOW  the aligned 8-key window holding the first four keys, one
+//                   or two 16-byte loads (single tables: C3's runs of four);
+//   EJ_KEYS_CHUNKS  the aligned 8-byte chunks holding them, one to three
+//                   loads (batched tables, whose runs are mostly of one or
+//                   two rows).
+enum { EJ_KEYS_WINDOW = 0, EJ_KEYS_CHUNKS = 1 };
+template <int KEYS = EJ_KEYS_WINDOW>
 __device__ __forceinline__ void ej_probe_prefetch(const ej_table_view& t, const EjProbeWarp& w,
                                                   int32_t (&kk)[PR_ITEMS][PW_PREFETCH]) {
   static_assert(PW_PREFETCH == 4, "the window holds 4 keys past any offset");
+  constexpr bool chunks = KEYS == EJ_KEYS_CHUNKS;
   const int4* rk4 = reinterpret_cast<const int4*>(t.rkey - t.voff);
+  const int2* rk2 = reinterpret_cast<const int2*>(t.rkey - t.voff);
   int4 qa[PR_ITEMS], qb[PR_ITEMS];
   uint32_t o[PR_ITEMS];
 #pragma unroll
@@ -106,9 +116,21 @@ __device__ __forceinline__ void ej_probe_prefetch(const ej_table_view& t, const 
     o[j] = 0;
     if (w.lo[j] != NULL_RUN && w.cnt[j]) {
       const uint32_t p = w.lo[j] + t.voff;
-      o[j] = p & 3u;
-      qa[j] = __ldg(rk4 + p / 4);
-      if (o[j] + min(w.cnt[j], (uint32_t)PW_PREFETCH) > 4u) qb[j] = __ldg(rk4 + p / 4 + 1);
+      if (chunks) {  // keys p .. p + min(cnt, 4) - 1 from the 8-byte chunks holding them
+        const uint32_t last = (p + min(w.cnt[j], (uint32_t)PW_PREFETCH) - 1u) / 2u;
+        o[j] = p & 1u;
+        const int2 a = __ldg(rk2 + p / 2);
+        int2 b = make_int2(EJ_NULL_KEY, EJ_NULL_KEY), c = b;
+        if (last >= p / 2 + 1u) b = __ldg(rk2 + p / 2 + 1);
+        if (last >= p / 2 + 2u) c = __ldg(rk2 + p / 2 + 2);
+        qa[j] = make_int4(a.x, a.y, b.x, b.y);
+        qb[j].x = c.x;
+        qb[j].y = c.y;
+      } else {
+        o[j] = p & 3u;
+        qa[j] = __ldg(rk4 + p / 4);
+        if (o[j] + min(w.cnt[j], (uint32_t)PW_PREFETCH) > 4u) qb[j] = __ldg(rk4 + p / 4 + 1);
+      }
     }
   }
 #pragma unroll
