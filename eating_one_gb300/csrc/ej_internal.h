@@ -181,6 +181,9 @@ struct ej_table_view {
   uint64_t nR = 0;
   uint32_t hb = 1;
   uint32_t voff = 0;  // rval - voff is 16-byte aligned (tables of a batch share one array)
+  // known on the host to have runs of about one row (an index whose build
+  // chose bucket bounds for its short runs): probes load run keys in 8-byte chunks
+  uint32_t short_runs = 0;
 };
 uint32_t ej_table_bucket_bits(uint64_t nR, int delta = 0);
 // the bucket-bits delta and the S partition bits (-1: planner) that apply to a

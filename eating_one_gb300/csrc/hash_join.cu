@@ -208,8 +208,9 @@ probe_write_kernel(const ej_tuple* __restrict__ P, const uint2* __restrict__ des
 // cursor, and writes them through its staging buffer as the write pass does.
 // Warps take their row ranges in the order they reach the cursor, so the row
 // order is not deterministic (the multiset is); rows at or past cap are
-// dropped, the cursor ends at the exact count.
-template <int KIND, bool OUTER>
+// dropped, the cursor ends at the exact count.  KEYS: how the run keys are
+// loaded (ej_probe_prefetch), fixed per table by the host.
+template <int KIND, bool OUTER, int KEYS>
 __global__ void __launch_bounds__(PR_THREADS)
 probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, uint64_t nwtiles,
                    unsigned long long* __restrict__ cursor, ej_result* __restrict__ out, uint64_t cap,
@@ -229,7 +230,7 @@ probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   // the run keys and the row reservation travel together: the key loads are
   // issued first and do not wait for the atomic's answer
   int32_t kk[PR_ITEMS][PW_PREFETCH];
-  ej_probe_prefetch(t, pw, kk);
+  ej_probe_prefetch<KEYS>(t, pw, kk);
   unsigned long long off = 0;
   if (lane == 0) {
     off = atomicAdd(cursor, total);
@@ -466,8 +467,12 @@ void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint
 template <int KIND, bool OUTER>
 static ej_status launch_fused(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                               unsigned long long* cursor, ej_result* out, uint64_t cap) {
-  probe_fused_kernel<KIND, OUTER><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(
-      P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 32);
+  if (t.short_runs)
+    probe_fused_kernel<KIND, OUTER, EJ_KEYS_CHUNKS><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(
+        P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 32);
+  else
+    probe_fused_kernel<KIND, OUTER, EJ_KEYS_WINDOW><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(
+        P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 32);
   return ej_check_launch(h, "probe_fused_kernel");
 }
 

@@ -103,7 +103,13 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
   ej_phase_begin(h);
   ej_status st = ej_table_build(h, tp, R, ix->rkey, ix->rval, ix->aux, &ix->view);
   for (int k = 1; k <= EJ_PHASES; k++) ej_phase_mark(h, k);
+  uint32_t bits = 1;
+  if (st == EJ_OK && ix->view.dir)  // the build's choice: bits = 0 when it took bucket bounds for short runs
+    st = cudaMemcpyAsync(&bits, ix->view.dir_bits, sizeof bits, cudaMemcpyDeviceToHost, h->stream) == cudaSuccess
+             ? EJ_OK
+             : ej_fail(h, EJ_ERR_CUDA, "reading the index header failed");
   if (st == EJ_OK) st = ej_finish(h, nullptr);
+  if (st == EJ_OK) ix->view.short_runs = bits == 0 ? 1u : 0u;
   if (st != EJ_OK) {
     cudaStreamSynchronize(h->stream);
     index_release(ix, h->stream);
