@@ -210,33 +210,24 @@ def _cpu_rels(scale: int):
     from eating_one_gb300.workloads import workload
     from oracle import oracle as O
 
-    return [(O.generate(workload(v, scale)["R"]), O.generate(workload(v, scale)["S"])) for v in VARIANTS]
+    nt = os.cpu_count() or 1
+    return [(O.generate(workload(v, scale)["R"], nt), O.generate(workload(v, scale)["S"], nt)) for v in VARIANTS]
 
 
 def cpu_baseline_sample(scale: int = 4, rels=None) -> dict:
-    """The oracle's hash_cpu restatement on a 1/2^scale-size sample of every
-    variant (generation excluded, as the reference times it), one thread each."""
+    """The oracle's hash_cpu restatement, single-threaded as the reference
+    runs it, on a 1/2^scale-size sample of every variant, one after another
+    (generation excluded, as the reference times it)."""
     rels = rels or _cpu_rels(scale)
-    results = [None] * len(rels)
-
-    def one(i):
-        R, S = rels[i]
-        dt, n = _cpu_join_timed(R, S, 0)
-        results[i] = (dt, len(R) + len(S), n)
-
-    threads = [threading.Thread(target=one, args=(i,)) for i in range(len(rels))]
-    for t in threads:
-        t.start()
-    for t in threads:
-        t.join()
-    wall = max(r[0] for r in results)
-    tuples = sum(r[1] for r in results)
-    return {"value": tuples / wall, "unit": UNIT, "cores": len(rels), "kind": "port",
+    results = [_cpu_join_timed(R, S, 0) for R, S in rels]
+    secs = sum(r[0] for r in results)
+    tuples = sum(len(R) + len(S) for R, S in rels)
+    return {"value": tuples / secs, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": "oracle restatement of joins/CPU_JOIN/hash_cpu (partition by val %% 2^20 + bucket "
                       "nested loop, rows materialised into a preallocated array) on the three C3 variants at "
-                      "1/%d size (R=2^%d, S=2^%d), one host thread per variant, generation excluded"
-                      % (2 ** scale, 26 - scale, 28 - scale),
-            "seconds": round(wall, 3), "rows": sum(r[2] for r in results)}
+                      "1/%d size (R=2^%d, S=2^%d), one host thread, the variants one after another, "
+                      "generation excluded" % (2 ** scale, 26 - scale, 28 - scale),
+            "seconds": round(secs, 3), "rows": sum(r[1] for r in results)}
 
 
 def run_reference(args) -> None:
@@ -410,18 +401,14 @@ def run_serve(n_requests: int, n_instances: int, lanes: int) -> None:
     del torch
 
 
-def run_configs(steps: int) -> None:
+def config_lines(eng, peaks: dict, steps: int, distance: bool) -> list[dict]:
     """The other configurations, each timed with CUDA events over `steps`
-    device-resident runs after warm-up; one JSON line per configuration."""
+    device-resident runs after warm-up: C1, C2, the C4 index, outer and star
+    joins and (distance) the 2-D/3-D distance joins; one dict per configuration."""
     import torch
 
-    from eating_one_gb300.build import build
-    from eating_one_gb300.engine import Engine
     from eating_one_gb300.workloads import workload
 
-    build()
-    eng = Engine(0)
-    peaks = load_peaks()
     props = torch.cuda.get_device_properties(0)
     stream = torch.cuda.current_stream()
 
@@ -443,14 +430,13 @@ def run_configs(steps: int) -> None:
                 "peak_source": peaks["source"]}
 
     lines = []
-    # C1: the parity configuration at full size
+    # C1: the parity configuration at full size (count sizes the output, then the join writes it)
     w = workload("c1")
     R, S = eng.generate(w["R"]), eng.generate(w["S"])
     n = eng.count("hash", R, S)
-    out = torch.empty((n, 4), dtype=torch.int32, device="cuda")
-    ms = timed(lambda: eng.hash_join(R, S, out=out))
-    lines.append({"config": "C1 hash join R=2^20 unique x S=2^22", "ms": round(ms, 4), "rows": n,
-                  "tuples_per_s": (R.shape[0] + S.shape[0]) / (ms / 1000),
+    ms = timed(lambda: eng.hash_join(R, S))
+    lines.append({"config": "C1 hash join R=2^20 unique x S=2^22 (count, then write)", "ms": round(ms, 4),
+                  "rows": n, "tuples_per_s": (R.shape[0] + S.shape[0]) / (ms / 1000),
                   "roofline": hbm(24 * (R.shape[0] + S.shape[0]) + 16 * n, ms)})
     # C2: block nested loop, all 2^36 pairs
     w = workload("c2")
@@ -465,6 +451,7 @@ def run_configs(steps: int) -> None:
                   "roofline": {"bound": "int32 issue", "peak_lane_ops_per_s": issue,
                                "frac_at_one_op_per_compare": round(pairs / (ms / 1000) / issue, 4)},
                   "reference_gpu_log": "2^20 x 2^16 in 1.483 s (nestLoopJoin, sm_35)"})
+    del out
     # C4: index joins, outer join, star join
     w = workload("c4")
     R, S = eng.generate(w["R"]), eng.generate(w["S"])
@@ -485,6 +472,7 @@ def run_configs(steps: int) -> None:
     lines.append({"config": "C4 left outer join R=2^24 x S=2^26", "ms": round(ms, 4), "rows": n,
                   "tuples_per_s": (R.shape[0] + S.shape[0]) / (ms / 1000),
                   "roofline": hbm(24 * (R.shape[0] + S.shape[0]) + 16 * n, ms)})
+    del out
     w = workload("c4_star")
     t = {k: eng.generate(v) for k, v in w.items()}
     args = (t["F1"], t["F2"], t["D1"], t["D2"])
@@ -495,6 +483,9 @@ def run_configs(steps: int) -> None:
     lines.append({"config": "C4 star join F=2^26 x D1, D2 = 2^20", "ms": round(ms, 4), "rows": n,
                   "tuples_per_s": (2 * t["F1"].shape[0] + nd) / (ms / 1000),
                   "roofline": hbm(8 * nd + 16 * t["F1"].shape[0] + 32 * n, ms)})
+    del out, t
+    if not distance:
+        return lines
     # distance joins: all 2^38 pairs of 2^19 x 2^19 reference-shaped points, radius 1
     from eating_one_gb300.native import point_result_dtype
     from eating_one_gb300.workloads import distance_workload
@@ -521,7 +512,17 @@ def run_configs(steps: int) -> None:
                       "cpu_baseline": {"pairs_per_s": len(Rp) * len(s_sample) / cpu_s, "cores": threads,
                                        "kind": "port", "sample": "R=2^19 x the first 1024 S points"},
                       "reference_cpu_log": "2-D 2^19 x 2^19 in 3718 s (complex_block/2d_cpu/nohup.out)"})
-    for ln in lines:
+    return lines
+
+
+def run_configs(steps: int) -> None:
+    """`--configs`: every other configuration, one JSON line each, distance joins included."""
+    from eating_one_gb300.build import build
+    from eating_one_gb300.engine import Engine
+
+    build()
+    eng = Engine(0)
+    for ln in config_lines(eng, load_peaks(), steps, distance=True):
         print(json.dumps(ln), flush=True)
 
 
@@ -533,6 +534,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="leave out the C1, C2 and C4 timings")
     ap.add_argument("--profile", default=None, help="run a small profiling case of this workload instead")
     ap.add_argument("--scale", type=int, default=3)
     ap.add_argument("--repeat", type=int, default=3)
@@ -582,15 +584,21 @@ def main() -> None:
         for side in ("R", "S"):
             w[side].seed ^= (rank * 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
         R, S = eng.generate(w["R"]), eng.generate(w["S"])
-        n_out = eng.count("hash", R, S)
-        out = torch.empty((n_out, 4), dtype=torch.int32, device="cuda")
-        joins.append({"name": v, "R": R, "S": S, "n_out": n_out, "out": out,
-                      "d_count": torch.zeros(1, dtype=torch.int64, device="cuda")})
+        joins.append({"name": v, "R": R, "S": S, "out": None, "n_out": None})
     units = sum(j["R"].shape[0] + j["S"].shape[0] for j in joins)
 
     def step():
+        # the reference's sequence per join (hj.cc:997-1115): the count pass,
+        # the count read back to the host, an output of exactly that size, the
+        # write (which reuses the count's table, partitioned S and run
+        # descriptors); the previous step's output is released first, so the
+        # caching allocator hands the same memory back
         for j in joins:
-            eng.hash_join_async(j["R"], j["S"], j["out"], j["d_count"])
+            j["out"] = None
+            n = eng.count("hash", j["R"], j["S"])
+            j["out"] = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+            j["n_out"] = n
+            eng.hash_join(j["R"], j["S"], out=j["out"])
 
     for _ in range(args.warmup):
         step()
@@ -616,31 +624,49 @@ def main() -> None:
     if dist:
         dist.barrier()
     launches = eng.kernel_launches() - launches0
-    phases, njoins = eng.phase_totals()
+    phases, _ = eng.phase_totals()
     eng.set_timing(False)
-    clk = clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
 
-    # every timed join must have produced exactly the counted rows, without device errors
+    # every join's rows against the oracle's full-size digest (count and
+    # order-independent checksum, tests/golden/fullsize.json); other ranks'
+    # relations are seeded differently, so there only the count is checked
+    # against the join's own count pass
     status = eng.sync_status()
-    for j in joins:
-        assert int(j["d_count"].item()) == j["n_out"], (j["name"], int(j["d_count"].item()), j["n_out"])
     assert status == 0, "device status %d: %s" % (status, eng.last_error())
+    parity = {}
+    gold = {}
+    gpath = os.path.join(ROOT, "tests", "golden", "fullsize.json")
+    if rank == 0 and os.path.exists(gpath):
+        with open(gpath) as f:
+            gold = json.load(f)
+    for j in joins:
+        got = {"count": int(j["out"].shape[0]), "checksum": eng.checksum(j["out"])}
+        want = gold.get(j["name"], {}).get("inner")
+        if want is not None:
+            assert got == want, (j["name"], got, want)
+            parity[j["name"]] = "count %d and checksum %d equal to the oracle's" % (got["count"], got["checksum"])
 
     per_rank = gather_ms(ms, dist, torch.device("cuda", local))
     value, ms_max = aggregate(per_rank, units, 1)
 
     # roofline of the dominant phase (per join, averaged over the timed joins)
+    nj = len(joins) * args.steps
     n_s = sum(j["S"].shape[0] for j in joins) / len(joins)
     n_r = sum(j["R"].shape[0] for j in joins) / len(joins)
     n_o = sum(j["n_out"] for j in joins) / len(joins)
     names = ["build (R table: LSD radix passes + key directory)", "partition (S radix pass)",
-             "count (none: the probe is one pass)", "probe (probe_fused_kernel: find, reserve, write)"]
+             "count (probe_count_kernel: every probe's run, stored as a descriptor; scan of the warp-tile totals)",
+             "write (probe_write_kernel: rows from the run descriptors at the scanned offsets)"]
     kernel = ["rx_scatter_kernel+rx_hist_kernel (R)", "rx_scatter_kernel+rx_hist_kernel (S)",
-              "probe_count_kernel", "probe_fused_kernel"]
-    # algorithmic bytes per launch of each phase
-    phase_bytes = [24.0 * n_r * 3 + 4.0 * n_r, 24.0 * n_s, 8.0 * n_s, 8.0 * n_s + 16.0 * n_o]
-    per_join = [p / max(njoins, 1) for p in phases]
+              "probe_count_kernel", "probe_write_kernel"]
+    # algorithmic bytes per launch of each phase: the build reads R once and
+    # writes its two columns (16 B per row), the partition reads and writes S
+    # (16 B per tuple), the count reads the probe and writes its descriptor
+    # (16 B per probe), the write reads the probe and its descriptor and writes
+    # the rows (16 B per probe + 16 B per row)
+    phase_bytes = [16.0 * n_r, 16.0 * n_s, 16.0 * n_s, 16.0 * n_s + 16.0 * n_o]
+    per_join = [p / nj for p in phases]
     dom = max(range(4), key=lambda i: per_join[i])
     achieved = phase_bytes[dom] / (per_join[dom] / 1000.0) / 1e9
     traffic = None
@@ -651,10 +677,22 @@ def main() -> None:
     alg = sum(alg_bytes("hash", j["R"].shape[0], j["S"].shape[0], j["n_out"]) for j in joins)
     join_gbs = alg / (ms_max / 1000.0) / 1e9
 
+    # the other configurations (C1, C2, C4), device-timed on the same GPU
+    secondary = None
+    if rank == 0 and not args.no_secondary:
+        for j in joins:
+            j["out"] = None
+        torch.cuda.empty_cache()
+        secondary = config_lines(eng, peaks, 10, distance=False)
+    clk = clocks.stop()
+
     # end to end through the host-buffer C ABI call
     e2e = None
     if args.e2e_steps > 0:
         hosts = []
+        for j in joins:
+            j["out"] = None
+        torch.cuda.empty_cache()
         max_out = max(j["n_out"] for j in joins)
         out_h = torch.empty((max_out, 4), dtype=torch.int32, pin_memory=True)
         for j in joins:
@@ -677,7 +715,8 @@ def main() -> None:
         d2h = int(sum(16 * n for _, _, n in hosts))
         e2e = {"value": units * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "ms_per_step": round(e2e_s * 1000.0, 3),
-               "api": "ej_join_host_chunked (pinned host R, S and out; 2^25-row S chunks)",
+               "api": "ej_join_host_chunked (pinned host R, S and out; 2^25-row S chunks, each chunk counted "
+                      "before its rows are written)",
                "link": dict(link, floor_ms=round(1000.0 * max(h2d / (link["both_gbs"] * 1e9),
                                                                d2h / (link["both_gbs"] * 1e9)), 2))}
 
@@ -694,16 +733,24 @@ def main() -> None:
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded device generators)",
         "config": {"workload": WORKLOAD, "R": 1 << 26, "S": 1 << 28, "joins_per_step": len(joins),
                    "results_per_step": int(sum(j["n_out"] for j in joins)),
+                   "step": "per join: count pass (ej_hash_join_count: R table build, S partition, count "
+                           "with run descriptors, scan), count read back, output of that size, write "
+                           "(ej_hash_join, from the count's descriptors)",
                    "l2": "inputs larger than L2 (R 512 MB, S 2 GB per join)", "parallelism": "dp%d" % world},
+        "parity": parity,
         "roofline": {"bound": "hbm", "kernel": kernel[dom], "phase": names[dom],
                      "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+                     "traffic_source": "not measured in this run: dram__bytes_read.sum + dram__bytes_write.sum "
+                                       "of a 1/8-size ncu capture of the same kernel, scaled by 8 "
+                                       "(profiles/traffic_c3.json)",
                      "peak_source": peaks["source"],
                      "bytes_per_launch": int(phase_bytes[dom]), "ms_per_launch": round(per_join[dom], 4)},
         "join_roofline": {"alg_bytes_per_step": int(alg), "achieved": round(join_gbs, 1), "unit": "GB/s",
                           "frac": round(join_gbs / peaks["hbm_gbs"], 4), "peak_source": peaks["source"]},
         "phases_ms_per_join": {"build": round(per_join[0], 4), "partition": round(per_join[1], 4),
                                "count": round(per_join[2], 4), "write": round(per_join[3], 4)},
+        "secondary": secondary,
         "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)

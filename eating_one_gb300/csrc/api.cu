@@ -103,6 +103,7 @@ extern "C" ej_status ej_destroy(ej_handle* h) {
   cudaFree(h->d_batch_counts);
   cudaFreeHost(h->h_batch_counts);
   for (cudaEvent_t e : h->ring) cudaEventDestroy(e);
+  delete h->prep;
   delete h;
   return EJ_OK;
 }
@@ -120,6 +121,7 @@ extern "C" ej_status ej_trim(ej_handle* h) {
   EJ_CUDA(h, cudaSetDevice(h->device));
   EJ_CUDA(h, cudaStreamSynchronize(h->stream));
   ej_stream_release(h);
+  h->prep_valid = false;
   EJ_CUDA(h, cudaFree(h->arena));
   EJ_CUDA(h, cudaFree(h->stage));
   h->arena = h->stage = nullptr;
@@ -241,6 +243,7 @@ extern "C" ej_status ej_phase_totals(ej_handle* h, double ms[EJ_PHASES], uint32_
 }
 
 ej_status ej_arena_reserve(ej_handle* h, size_t bytes) {
+  h->prep_valid = false;  // every call that lays out the arena overwrites a kept count
   if (bytes <= h->arena_cap) return EJ_OK;
   EJ_CUDA(h, cudaStreamSynchronize(h->stream));
   if (h->arena) EJ_CUDA(h, cudaFree(h->arena));
@@ -323,8 +326,16 @@ static ej_status hash_join_sync(ej_handle* h, const ej_tuple* R, uint64_t nR, co
   else if (!out_count) return ej_fail(h, EJ_ERR_INVALID, "out_count is NULL");
   EJ_TRY(ej_hash_join_run(h, R, nR, S, nS, out, out_cap, h->d_words, mode));
   uint64_t count = 0;
-  EJ_TRY(ej_finish(h, &count));
+  const ej_status fs = ej_finish(h, &count);
+  if (fs != EJ_OK) {
+    h->prep_valid = false;
+    return fs;
+  }
   *out_count = count;
+  if (mode == 2 && h->prep_valid) {
+    h->prep->count_known = true;
+    h->prep->count = count;
+  }
   return mode == 2 ? EJ_OK : ej_capacity_result(h, count, out_cap);
 }
 

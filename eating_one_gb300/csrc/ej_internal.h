@@ -16,6 +16,10 @@ struct ej_dev_status {
   unsigned long long aux;
 };
 
+// the table, partitioned probe side and run descriptors that a hash-join
+// count leaves for the write of the same join (hash_join.cu)
+struct ej_prepared_join;
+
 struct ej_zipf_cache {
   double s = -1.0;
   uint32_t domain = 0;
@@ -60,6 +64,12 @@ struct ej_handle {
   unsigned long long* d_batch_counts = nullptr;
   unsigned long long* h_batch_counts = nullptr;
   uint32_t batch_counts_cap = 0;
+  // a hash-join count kept for the write that follows it (ej_hash_join_count
+  // then ej_hash_join on the same relations); any other use of the arena
+  // drops it (ej_arena_reserve)
+  ej_prepared_join* prep = nullptr;
+  bool prep_valid = false;
+  bool opt_count_reuse = true;
 };
 
 // Arena layout: callers first add every buffer to a plan, then reserve once.

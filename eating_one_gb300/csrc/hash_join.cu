@@ -461,7 +461,8 @@ void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint
     L.spart_off = p.add((size_t)nS * sizeof(ej_tuple));
     ej_radix_plan_add(p, L.splan, nS);
   }
-  ej_probe_plan(p, L.pp, nS, !count_only && two_pass);
+  (void)count_only;
+  ej_probe_plan(p, L.pp, nS, two_pass);
 }
 
 template <int KIND, bool OUTER>
@@ -515,9 +516,32 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
   return EJ_OK;
 }
 
+// the rows of the join whose count the handle kept: the write pass alone,
+// from the count's run descriptors and warp-tile offsets
+static ej_status hash_join_write_kept(ej_handle* h, ej_result* out, uint64_t out_cap, unsigned long long* d_count) {
+  const ej_prepared_join& pj = *h->prep;
+  ej_phase_begin(h);
+  for (int k = 1; k <= 3; k++) ej_phase_mark(h, k);  // build, partition and count were the count's
+  EJ_TRY(ej_probe_write(h, pj.L.pp, pj.P, pj.t, out, out_cap));
+  const unsigned long long* woff = reinterpret_cast<const unsigned long long*>(ej_arena_at(h, pj.L.pp.off_off));
+  if (d_count)
+    EJ_CUDA(h, cudaMemcpyAsync(d_count, woff + pj.L.pp.nwtiles, sizeof(unsigned long long),
+                               cudaMemcpyDeviceToDevice, h->stream));
+  ej_phase_mark(h, 4);
+  // kept for another write only when this one was cut short by the capacity
+  h->prep_valid = pj.count_known && out_cap < pj.count;
+  return EJ_OK;
+}
+
 ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
                            ej_result* out, uint64_t out_cap, unsigned long long* d_count, int mode) {
   // mode: 0 = partition S when the planner says so, 1 = never partition S, 2 = count only
+  if (mode == 0 && h->prep_valid && h->prep && h->prep->arena == h->arena && h->prep->R == R &&
+      h->prep->nR == nR && h->prep->S == S && h->prep->nS == nS)
+    return hash_join_write_kept(h, out, out_cap, d_count);
+  // a count keeps its table, partitioned S and run descriptors for the write
+  // that follows it
+  const bool keep = mode == 2 && h->opt_count_reuse;
   const uint32_t pb = (mode == 1) ? 0u : ej_probe_partition_bits(h, nR, nS);
   ej_plan_bytes p;
   ej_table_plan_t tp;
@@ -525,12 +549,27 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   ej_probe_layout L;
   // the build-side-only join keeps its rows in probe order (the batched joins
   // give the same rows in the same order); the others take the one-pass probe
-  ej_probe_layout_add(p, L, nS, pb, mode == 2, /*two_pass=*/mode == 1);
+  ej_probe_layout_add(p, L, nS, pb, mode == 2, /*two_pass=*/mode == 1 || keep);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t;
   EJ_TRY(ej_table_build(h, tp, R, reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rkey_off)),
                         reinterpret_cast<int32_t*>(ej_arena_at(h, tp.rval_off)), ej_arena_at(h, tp.aux_off), &t));
   ej_phase_mark(h, 1);
-  return ej_probe_exec(h, L, t, S, /*outer=*/false, mode == 2, out, out_cap, d_count);
+  EJ_TRY(ej_probe_exec(h, L, t, S, /*outer=*/false, mode == 2, out, out_cap, d_count));
+  if (keep) {
+    if (!h->prep) h->prep = new ej_prepared_join();
+    ej_prepared_join& pj = *h->prep;
+    pj.R = R;
+    pj.nR = nR;
+    pj.S = S;
+    pj.nS = nS;
+    pj.arena = h->arena;
+    pj.P = L.pb ? reinterpret_cast<const ej_tuple*>(ej_arena_at(h, L.spart_off)) : S;
+    pj.L = L;
+    pj.t = t;
+    pj.count_known = false;
+    h->prep_valid = true;
+  }
+  return EJ_OK;
 }

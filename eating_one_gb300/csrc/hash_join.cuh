@@ -82,6 +82,22 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
                         bool outer, bool count_only, ej_result* out, uint64_t out_cap,
                         unsigned long long* d_count);
 
+// What a hash-join count leaves in the handle's arena for the write that
+// follows it: the table, the probe side as probed (S or its partitioned
+// copy) and the probe layout with its run descriptors and warp-tile offsets.
+struct ej_prepared_join {
+  const ej_tuple* R = nullptr;
+  uint64_t nR = 0;
+  const ej_tuple* S = nullptr;
+  uint64_t nS = 0;
+  const void* arena = nullptr;  // the arena allocation the state lives in
+  const ej_tuple* P = nullptr;  // the probes the count walked
+  ej_probe_layout L;
+  ej_table_view t;
+  bool count_known = false;  // the count reached the host (synchronous count call)
+  uint64_t count = 0;
+};
+
 // mode: 0 = partition S when the planner says so, 1 = never partition S, 2 = count only
 ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
                            ej_result* out, uint64_t out_cap, unsigned long long* d_count, int mode);

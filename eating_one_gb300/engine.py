@@ -139,6 +139,13 @@ class Engine:
     # ---- joins ------------------------------------------------------------------
     def join(self, algo: str, R: torch.Tensor, S: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         a = native.ALGO[algo]
+        if out is None and algo == "hash":
+            # the reference's sequence (hj.cc:997-1115): the count pass sizes the
+            # output, then the join writes it; the handle keeps the count's table,
+            # partitioned S and run descriptors, so the join only writes
+            out = torch.empty((self.count("hash", R, S), 4), dtype=torch.int32, device=self.device)
+            if out.shape[0] == 0:
+                return out
         return self._run_sized(lambda o, cap, cnt: self.lib.ej_join(
             self.h, a, _ptr(R), R.shape[0], _ptr(S), S.shape[0], o, cap, cnt), out, 4)
 

@@ -135,18 +135,31 @@ typedef struct {
   ejo_tuple* out;
 } mt_part_arg;
 
+/* Each thread counts into its own array and copies it into the shared
+ * partition-major layout afterwards.  The reference increments the shared
+ * LL[hash * THREAD_NUM + threadIdx] in place (thread-hash-bnlj.cc:174-176),
+ * so neighbouring threads write neighbouring words of one cache line on every
+ * row; the counts are the same either way, the private arrays only remove
+ * that false sharing (it kept 16 threads near the speed of one). */
 static void* mt_count(void* a_) {
   mt_part_arg* a = (mt_part_arg*)a_;
-  for (uint64_t i = a->lo; i < a->hi; i++) a->cnt[(uint64_t)((uint32_t)a->in[i].val % a->np) * a->nt + a->t]++;
+  uint64_t* mine = (uint64_t*)calloc(a->np, sizeof(uint64_t));
+  if (!mine) { a->out = NULL; return NULL; }
+  for (uint64_t i = a->lo; i < a->hi; i++) mine[(uint32_t)a->in[i].val % a->np]++;
+  for (uint32_t p = 0; p < a->np; p++) a->cnt[(uint64_t)p * a->nt + a->t] = mine[p];
+  free(mine);
   return NULL;
 }
 
+/* the scatter's running offsets, likewise thread-private (the reference's
+ * LLS[hash * THREAD_NUM + threadIdx]++, :211-213) */
 static void* mt_scatter(void* a_) {
   mt_part_arg* a = (mt_part_arg*)a_;
-  for (uint64_t i = a->lo; i < a->hi; i++) {
-    uint64_t* pos = &a->cnt[(uint64_t)((uint32_t)a->in[i].val % a->np) * a->nt + a->t];
-    a->out[(*pos)++] = a->in[i];
-  }
+  uint64_t* pos = (uint64_t*)malloc(sizeof(uint64_t) * a->np);
+  if (!pos) { a->out = NULL; return NULL; }
+  for (uint32_t p = 0; p < a->np; p++) pos[p] = a->cnt[(uint64_t)p * a->nt + a->t];
+  for (uint64_t i = a->lo; i < a->hi; i++) a->out[pos[(uint32_t)a->in[i].val % a->np]++] = a->in[i];
+  free(pos);
   return NULL;
 }
 
@@ -164,8 +177,11 @@ static int mt_partition(const ejo_tuple* in, uint64_t n, uint32_t np, uint32_t n
     args[t].lo = (uint64_t)t * chunk < n ? (uint64_t)t * chunk : n;
     args[t].hi = args[t].lo + chunk < n ? args[t].lo + chunk : n;
   }
+  int failed = 0;
   for (uint32_t t = 0; t < nt; t++) pthread_create(&th[t], NULL, mt_count, &args[t]);
   for (uint32_t t = 0; t < nt; t++) pthread_join(th[t], NULL);
+  for (uint32_t t = 0; t < nt; t++) failed |= args[t].out == NULL;
+  if (failed) { free(cnt); free(args); free(th); return -1; }
   uint64_t run = 0;
   for (uint64_t k = 0; k < (uint64_t)np * nt; k++) {
     const uint64_t c = cnt[k];
@@ -176,8 +192,9 @@ static int mt_partition(const ejo_tuple* in, uint64_t n, uint32_t np, uint32_t n
   start[np] = n;
   for (uint32_t t = 0; t < nt; t++) pthread_create(&th[t], NULL, mt_scatter, &args[t]);
   for (uint32_t t = 0; t < nt; t++) pthread_join(th[t], NULL);
+  for (uint32_t t = 0; t < nt; t++) failed |= args[t].out == NULL;
   free(cnt); free(args); free(th);
-  return 0;
+  return failed ? -1 : 0;
 }
 
 typedef struct {
@@ -660,4 +677,204 @@ uint64_t ejo_checksum(const int32_t* words, uint64_t nrows, uint32_t words_per_r
     sum += h;
   }
   return sum;
+}
+
+/* ---------------------------------------------------------------------------
+ * Digests of results too large to materialise (full-size configurations):
+ * the count and the order-independent checksum of a join's rows, computed
+ * row by row as the joins above find them but fed to the checksum instead of
+ * an output array.  The inner and left outer joins follow
+ * joins/multi_joins/hash (ejo_hash_join_mt: partition both sides by
+ * val % partitions, threads take partitions from a shared counter and
+ * nested-loop each partition's S rows against its R rows); every S row
+ * without a match adds its NULL-extended row when `outer` is set, as
+ * ejo_left_outer_join emits it.  The star join probes the same hash indexes
+ * as ejo_star_join3 (joins/CPU_JOIN/inner_cpu/inner-idx-bnlj.cc:142-185),
+ * fact rows split over the threads.  The multiset of rows, and so the digest,
+ * is that of the single-threaded joins.
+ * ------------------------------------------------------------------------- */
+static inline uint64_t row_mix4(int32_t a, int32_t b, int32_t c, int32_t d) {
+  uint64_t h = 0x243F6A8885A308D3ull;
+  h = ej_splitmix64(h ^ (uint64_t)(uint32_t)a);
+  h = ej_splitmix64(h ^ (uint64_t)(uint32_t)b);
+  h = ej_splitmix64(h ^ (uint64_t)(uint32_t)c);
+  return ej_splitmix64(h ^ (uint64_t)(uint32_t)d);
+}
+
+typedef struct {
+  const ejo_tuple *pr, *ps;
+  const uint64_t *rstart, *sstart;
+  uint32_t np;
+  int outer;
+  uint32_t* next;
+  uint64_t count, sum;
+} digest_arg;
+
+static void* digest_join(void* a_) {
+  digest_arg* a = (digest_arg*)a_;
+  uint64_t count = 0, sum = 0;
+  for (;;) {
+    const uint32_t p = __atomic_fetch_add(a->next, 1u, __ATOMIC_RELAXED);
+    if (p >= a->np) break;
+    const ejo_tuple* r0 = a->pr + a->rstart[p];
+    const uint64_t nr = a->rstart[p + 1] - a->rstart[p];
+    for (uint64_t i = a->sstart[p]; i < a->sstart[p + 1]; i++) {
+      const ejo_tuple s = a->ps[i];
+      uint64_t m = 0;
+      for (uint64_t j = 0; j < nr; j++) {
+        if (r0[j].val != s.val) continue;
+        sum += row_mix4(r0[j].key, r0[j].val, s.key, s.val);
+        m++;
+      }
+      if (a->outer && m == 0) {
+        sum += row_mix4(EJO_NULL, EJO_NULL, s.key, s.val);
+        m = 1;
+      }
+      count += m;
+    }
+  }
+  a->count = count;
+  a->sum = sum;
+  return NULL;
+}
+
+int ejo_join_digest_mt(const ejo_tuple* R, uint64_t nR, const ejo_tuple* S, uint64_t nS, int outer,
+                       uint32_t partitions, uint32_t nthreads, uint64_t* count, uint64_t* checksum) {
+  if (partitions == 0) partitions = 1u << 20;
+  if (nthreads == 0) nthreads = 8;
+  int rc = -1;
+  ejo_tuple* pr = (ejo_tuple*)malloc(sizeof(ejo_tuple) * (nR ? nR : 1));
+  ejo_tuple* ps = (ejo_tuple*)malloc(sizeof(ejo_tuple) * (nS ? nS : 1));
+  uint64_t* rstart = (uint64_t*)malloc(sizeof(uint64_t) * ((uint64_t)partitions + 1));
+  uint64_t* sstart = (uint64_t*)malloc(sizeof(uint64_t) * ((uint64_t)partitions + 1));
+  digest_arg* args = (digest_arg*)calloc(nthreads, sizeof(digest_arg));
+  pthread_t* th = (pthread_t*)calloc(nthreads, sizeof(pthread_t));
+  uint32_t next = 0;
+  if (!pr || !ps || !rstart || !sstart || !args || !th) goto done;
+  if (mt_partition(R, nR, partitions, nthreads, pr, rstart) || mt_partition(S, nS, partitions, nthreads, ps, sstart))
+    goto done;
+  for (uint32_t t = 0; t < nthreads; t++) {
+    args[t].pr = pr; args[t].ps = ps; args[t].rstart = rstart; args[t].sstart = sstart;
+    args[t].np = partitions; args[t].outer = outer; args[t].next = &next;
+    pthread_create(&th[t], NULL, digest_join, &args[t]);
+  }
+  *count = 0;
+  *checksum = 0;
+  for (uint32_t t = 0; t < nthreads; t++) {
+    pthread_join(th[t], NULL);
+    *count += args[t].count;
+    *checksum += args[t].sum;
+  }
+  rc = 0;
+done:
+  free(pr); free(ps); free(rstart); free(sstart); free(args); free(th);
+  return rc;
+}
+
+typedef struct {
+  const ejo_tuple *F1, *F2, *D1, *D2;
+  uint64_t f0, f1;
+  const ejo_hash_index *i1, *i2;
+  uint64_t count, sum;
+} star_digest_arg;
+
+static void* star_digest(void* a_) {
+  star_digest_arg* a = (star_digest_arg*)a_;
+  const ejo_hash_index *i1 = a->i1, *i2 = a->i2;
+  uint64_t count = 0, sum = 0;
+  for (uint64_t f = a->f0; f < a->f1; f++) {
+    const ejo_tuple x = a->F1[f], y = a->F2[f];
+    const uint32_t h1 = (uint32_t)x.val % i1->nb, h2 = (uint32_t)y.val % i2->nb;
+    for (uint64_t u = 0; u < i1->idxcount[h1]; u++) {
+      const ejo_bucket* b1 = &i1->bucket[i1->buck_array[h1] + u];
+      if (b1->val != x.val) continue;
+      for (uint64_t v = 0; v < i2->idxcount[h2]; v++) {
+        const ejo_bucket* b2 = &i2->bucket[i2->buck_array[h2] + v];
+        if (b2->val != y.val) continue;
+        const ejo_tuple d1 = a->D1[b1->adr], d2 = a->D2[b2->adr];
+        const int32_t w[8] = {d1.key, d1.val, x.key, x.val, d2.key, d2.val, y.key, y.val};
+        uint64_t h = 0x243F6A8885A308D3ull;
+        for (int k = 0; k < 8; k++) h = ej_splitmix64(h ^ (uint64_t)(uint32_t)w[k]);
+        sum += h;
+        count++;
+      }
+    }
+  }
+  a->count = count;
+  a->sum = sum;
+  return NULL;
+}
+
+int ejo_star_digest_mt(const ejo_tuple* F1, const ejo_tuple* F2, uint64_t nF, const ejo_tuple* D1, uint64_t nD1,
+                       const ejo_tuple* D2, uint64_t nD2, uint32_t nb_bucket, uint32_t nthreads, uint64_t* count,
+                       uint64_t* checksum) {
+  if (nb_bucket == 0) nb_bucket = 1u << 20;
+  if (nthreads == 0) nthreads = 8;
+  ejo_hash_index i1, i2;
+  int ok = hash_index_build(D1, nD1, nb_bucket, &i1) == 0;
+  ok = (hash_index_build(D2, nD2, nb_bucket, &i2) == 0) && ok;
+  star_digest_arg* args = (star_digest_arg*)calloc(nthreads, sizeof(star_digest_arg));
+  pthread_t* th = (pthread_t*)calloc(nthreads, sizeof(pthread_t));
+  int rc = -1;
+  if (ok && args && th) {
+    for (uint32_t t = 0; t < nthreads; t++) {
+      star_digest_arg* a = &args[t];
+      a->F1 = F1; a->F2 = F2; a->D1 = D1; a->D2 = D2; a->i1 = &i1; a->i2 = &i2;
+      a->f0 = nF * t / nthreads;
+      a->f1 = nF * (t + 1) / nthreads;
+      pthread_create(&th[t], NULL, star_digest, a);
+    }
+    *count = 0;
+    *checksum = 0;
+    for (uint32_t t = 0; t < nthreads; t++) {
+      pthread_join(th[t], NULL);
+      *count += args[t].count;
+      *checksum += args[t].sum;
+    }
+    rc = 0;
+  }
+  hash_index_free(&i1);
+  hash_index_free(&i2);
+  free(args);
+  free(th);
+  return rc;
+}
+
+/* ejo_generate over row ranges in parallel (the rows are a pure function of
+ * the spec and the index, so the result is the same) */
+typedef struct {
+  const ej_gen_spec* sp;
+  ejo_tuple* out;
+  uint64_t lo, hi;
+} gen_arg;
+
+static void* gen_range(void* a_) {
+  gen_arg* a = (gen_arg*)a_;
+  for (uint64_t i = a->lo; i < a->hi; i++) {
+    a->out[i].key = (int32_t)((uint32_t)a->sp->key_base + (uint32_t)i);
+    a->out[i].val = ej_gen_val(a->sp, i);
+  }
+  return NULL;
+}
+
+void ejo_generate_mt(const ej_gen_spec* sp, ejo_tuple* out, uint32_t nthreads) {
+  if (nthreads == 0) nthreads = 1;
+  gen_arg* args = (gen_arg*)calloc(nthreads, sizeof(gen_arg));
+  pthread_t* th = (pthread_t*)calloc(nthreads, sizeof(pthread_t));
+  if (!args || !th) {
+    free(args);
+    free(th);
+    ejo_generate(sp, out);
+    return;
+  }
+  for (uint32_t t = 0; t < nthreads; t++) {
+    args[t].sp = sp;
+    args[t].out = out;
+    args[t].lo = sp->n * t / nthreads;
+    args[t].hi = sp->n * (t + 1) / nthreads;
+    pthread_create(&th[t], NULL, gen_range, &args[t]);
+  }
+  for (uint32_t t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  free(args);
+  free(th);
 }

@@ -62,6 +62,12 @@ def load() -> C.CDLL:
         lib.ejo_checksum.restype = u64
         lib.ejo_distance_join.argtypes = [u32, vp, u64, vp, u64, C.c_double, vp, u64, u32]
         lib.ejo_distance_join.restype = u64
+        pu64 = C.POINTER(u64)
+        lib.ejo_join_digest_mt.argtypes = [vp, u64, vp, u64, C.c_int, u32, u32, pu64, pu64]
+        lib.ejo_join_digest_mt.restype = C.c_int
+        lib.ejo_star_digest_mt.argtypes = [vp, vp, u64, vp, u64, vp, u64, u32, u32, pu64, pu64]
+        lib.ejo_star_digest_mt.restype = C.c_int
+        lib.ejo_generate_mt.argtypes = [vp, vp, u32]
         _lib = lib
     return _lib
 
@@ -76,10 +82,11 @@ def _rel(a) -> np.ndarray:
     return a
 
 
-def generate(spec) -> np.ndarray:
+def generate(spec, threads: int = 1) -> np.ndarray:
     """Host copy of a generated relation (same generator as the device).
 
-    Zipf specs with s > 0 get their CDF table built here (ejo_zipf_cdf)."""
+    Zipf specs with s > 0 get their CDF table built here (ejo_zipf_cdf).
+    threads > 1 generates row ranges in parallel (same rows)."""
     lib = load()
     out = np.empty((spec.n, 2), dtype=np.int32)
     keep = None
@@ -88,12 +95,39 @@ def generate(spec) -> np.ndarray:
         lib.ejo_zipf_cdf(spec.zipf_s, spec.domain, keep.ctypes.data)
         spec.cdf = keep.ctypes.data
     try:
-        if spec.n:
+        if spec.n and threads > 1:
+            lib.ejo_generate_mt(C.byref(spec), out.ctypes.data, threads)
+        elif spec.n:
             lib.ejo_generate(C.byref(spec), out.ctypes.data)
     finally:
         if keep is not None:
             spec.cdf = None
     return out
+
+
+def join_digest(R, S, outer: bool = False, threads: int = 0, partitions: int = 1 << 20) -> tuple[int, int]:
+    """(count, checksum) of the inner join (outer: the left outer join) of R
+    and S without materialising its rows: the joins/multi_joins/hash
+    restatement with every row fed to the order-independent checksum."""
+    lib = load()
+    R, S = _rel(R), _rel(S)
+    nt = threads or os.cpu_count() or 8
+    n, c = C.c_uint64(0), C.c_uint64(0)
+    if lib.ejo_join_digest_mt(_p(R), len(R), _p(S), len(S), int(outer), partitions, nt, C.byref(n), C.byref(c)):
+        raise MemoryError("ejo_join_digest_mt")
+    return int(n.value), int(c.value)
+
+
+def star_digest(F1, F2, D1, D2, threads: int = 0, nb_bucket: int = 1 << 20) -> tuple[int, int]:
+    """(count, checksum) of the 3-way star join without materialising its rows."""
+    lib = load()
+    F1, F2, D1, D2 = (_rel(x) for x in (F1, F2, D1, D2))
+    nt = threads or os.cpu_count() or 8
+    n, c = C.c_uint64(0), C.c_uint64(0)
+    if lib.ejo_star_digest_mt(_p(F1), _p(F2), len(F1), _p(D1), len(D1), _p(D2), len(D2), nb_bucket, nt,
+                              C.byref(n), C.byref(c)):
+        raise MemoryError("ejo_star_digest_mt")
+    return int(n.value), int(c.value)
 
 
 def _join(name: str, R, S, extra=()) -> np.ndarray:

@@ -94,3 +94,9 @@ def distance_cases():
         d["S"] = z[r["case"] + "_S"].view(point_dtype(r["dims"])).reshape(-1)
         out.append(d)
     return out
+
+
+def fullsize():
+    """The oracle's (count, checksum) of every full-size workload (tests/golden/make_fullsize.py)."""
+    with open(os.path.join(HERE, "fullsize.json")) as f:
+        return json.load(f)

@@ -169,6 +169,48 @@ def test_capacity_and_guard(engine):
     assert engine.count("hash", dev(R), dev(S)) == total
 
 
+@pytest.mark.parametrize("pb", [-1, 0, 6])
+def test_count_then_join_writes_from_the_count(engine, pb):
+    """ej_hash_join_count then ej_hash_join on the same relations, as the
+    reference sizes its output (hj.cc:997-1115): the join writes from the
+    count's table, partitioned S and run descriptors (one launch); a write cut
+    short by the capacity keeps them for the retry; any other call that lays
+    out the handle's scratch drops them, and the join then runs whole."""
+    rng = np.random.default_rng(50 + pb)
+    R, S = rel(rng, 50000, 0, 30000), rel(rng, 200003, 0, 40000, key_base=50000)
+    ref = O.hash_join(R, S)
+    Rd, Sd = dev(R), dev(S)
+    engine.set_option("partition_bits", pb)
+    try:
+        n = engine.count("hash", Rd, Sd)
+        assert n == len(ref)
+        out = torch.full((n + 64, 4), -7, dtype=torch.int32, device="cuda")
+        before = engine.kernel_launches()
+        with pytest.raises(JoinError) as ei:
+            engine.hash_join(Rd, Sd, out=out[: n // 2])
+        assert ei.value.status == native.EJ_ERR_CAPACITY
+        assert torch.all(out[n // 2:] == -7)
+        got = engine.hash_join(Rd, Sd, out=out[:n])
+        assert engine.kernel_launches() - before == 2  # two write passes, nothing rebuilt
+        same_multiset(got, ref)
+        assert torch.all(out[n:] == -7)
+        # the kept count is spent: the next join runs whole
+        before = engine.kernel_launches()
+        same_multiset(engine.hash_join(Rd, Sd, out=out[:n]), ref)
+        assert engine.kernel_launches() - before > 1
+        # another call in between drops the kept count
+        assert engine.count("hash", Rd, Sd) == n
+        engine.exclusive_scan_u32(torch.ones(1000, dtype=torch.int32, device="cuda"))
+        before = engine.kernel_launches()
+        same_multiset(engine.hash_join(Rd, Sd, out=out[:n]), ref)
+        assert engine.kernel_launches() - before > 1
+        # as does a count of other relations
+        assert engine.count("hash", Rd, Sd[:1000]) == len(O.hash_join(R, S[:1000]))
+        same_multiset(engine.hash_join(Rd, Sd, out=out[:n]), ref)
+    finally:
+        engine.set_option("partition_bits", -1)
+
+
 @pytest.mark.parametrize("n,dup,s_rows", [(1 << 22, 1, 1 << 23), (1 << 22, 3, 1 << 23), (1 << 20, 1, 17 << 20)])
 def test_directory_or_buckets(engine, n, dup, s_rows):
     """A 2^22-row table keeps its key directory when its runs average two rows

@@ -143,3 +143,42 @@ def test_multithreaded_restatement(threads, partitions):
     R, S = golden.join_ori()
     rows = O.hash_join_mt(R, S, threads=threads, partitions=partitions)
     assert len(rows) == 1002230 and int(rows[:, 1].astype(np.int64).sum()) == 50438235
+
+
+@pytest.mark.parametrize("name", ["c3_s0.0", "c3_s1.0", "c4"])
+def test_digest_matches_materialised_join(name):
+    """The full-size goldens come from ejo_join_digest_mt: at a small size its
+    count and checksum equal those of the materialised single-threaded joins,
+    inner and left outer, for any thread and partition count."""
+    w = workload(name, 8)
+    R, S = O.generate(w["R"]), O.generate(w["S"], threads=3)
+    assert np.array_equal(S, O.generate(w["S"]))
+    inner, outer = O.hash_join(R, S), O.left_outer_join(R, S)
+    for threads, parts in ((1, 1 << 20), (3, 1 << 14), (8, 4099)):
+        assert O.join_digest(R, S, threads=threads, partitions=parts) == (len(inner), O.checksum(inner))
+        assert O.join_digest(R, S, outer=True, threads=threads, partitions=parts) == (len(outer), O.checksum(outer))
+
+
+def test_star_digest_matches_materialised_join():
+    w = workload("c4_star", 7)
+    t = {k: O.generate(v) for k, v in w.items()}
+    rows = O.star_join3(t["F1"], t["F2"], t["D1"], t["D2"])
+    for threads in (1, 5):
+        assert O.star_digest(t["F1"], t["F2"], t["D1"], t["D2"], threads=threads) == (len(rows), O.checksum(rows))
+
+
+def test_fullsize_goldens_cover_the_bench_workloads():
+    g = golden.fullsize()
+    for name in ("c3_s0.0", "c3_s0.75", "c3_s1.0"):
+        assert g[name]["R"] == 1 << 26 and g[name]["S"] == 1 << 28
+        assert 9.6e8 < g[name]["inner"]["count"] < 9.7e8
+    assert g["c4"]["outer"]["count"] == 1 << 26
+    assert g["c4_star"]["star"]["count"] == 1 << 26
+
+
+@pytest.mark.parametrize("threads", [1, 2, 5])
+def test_multithreaded_join_any_thread_count(threads):
+    rng = np.random.default_rng(threads)
+    R = np.stack([np.arange(3000), rng.integers(0, 500, 3000)], axis=1).astype(np.int32)
+    S = np.stack([np.arange(9000), rng.integers(-20, 520, 9000)], axis=1).astype(np.int32)
+    assert np.array_equal(O.canon(O.hash_join_mt(R, S, threads=threads, partitions=97)), O.canon(O.hash_join(R, S)))
