@@ -4,12 +4,26 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
 #include "ej_device.cuh"
 #include "hash_join.cuh"
 #include "ej_entry.h"
+
+// ---- allocation-failure injection (tests) ----------------------------------
+
+static std::atomic<uint32_t> g_alloc_failures{0};
+
+extern "C" void ej_inject_alloc_failures(uint32_t count) { g_alloc_failures.store(count); }
+
+bool ej_alloc_failure_injected() {
+  uint32_t c = g_alloc_failures.load(std::memory_order_relaxed);
+  while (c > 0)
+    if (g_alloc_failures.compare_exchange_weak(c, c - 1)) return true;
+  return false;
+}
 
 // ---- errors ---------------------------------------------------------------
 
@@ -73,10 +87,10 @@ extern "C" ej_status ej_create(int device, ej_handle** out) {
   int l2 = 0;
   cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device);
   h->l2_bytes = (size_t)l2;
-  bool ok = cudaMalloc(&h->d_status, sizeof(ej_dev_status)) == cudaSuccess &&
-            cudaMalloc(&h->d_words, 8 * sizeof(unsigned long long)) == cudaSuccess &&
-            cudaMallocHost(&h->h_words, 8 * sizeof(unsigned long long)) == cudaSuccess &&
-            cudaMallocHost(&h->h_status, sizeof(ej_dev_status)) == cudaSuccess;
+  bool ok = ej_dev_alloc(&h->d_status, sizeof(ej_dev_status)) == cudaSuccess &&
+            ej_dev_alloc(&h->d_words, 8 * sizeof(unsigned long long)) == cudaSuccess &&
+            ej_host_alloc(&h->h_words, 8 * sizeof(unsigned long long)) == cudaSuccess &&
+            ej_host_alloc(&h->h_status, sizeof(ej_dev_status)) == cudaSuccess;
   if (ok) ok = cudaMemset(h->d_status, 0, sizeof(ej_dev_status)) == cudaSuccess &&
                cudaMemset(h->d_words, 0, 8 * sizeof(unsigned long long)) == cudaSuccess;
   if (!ok) {
@@ -182,6 +196,15 @@ extern "C" ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value) {
       h->opt_bucket_delta = (int)value;
       h->opt_bucket_delta_set = value != 0;  // 0 hands the choice back to the tuning table
       return EJ_OK;
+    case EJ_OPT_WAIT_LIMIT_NS:
+      if (value < -1 || value > 10000000000ll) return ej_fail(h, EJ_ERR_INVALID, "wait limit must be -1..1e10 ns");
+      h->wait_limit_ns = value < 0 ? EJ_DEFAULT_WAIT_LIMIT_NS : (unsigned long long)value;
+      return EJ_OK;
+    case EJ_OPT_COUNT_REUSE:
+      if (value != 0 && value != 1) return ej_fail(h, EJ_ERR_INVALID, "count reuse is 0 or 1");
+      h->opt_count_reuse = value != 0;
+      if (!h->opt_count_reuse) h->prep_valid = false;
+      return EJ_OK;
   }
   return ej_fail(h, EJ_ERR_INVALID, "unknown option %d", (int)opt);
 }
@@ -250,7 +273,7 @@ ej_status ej_arena_reserve(ej_handle* h, size_t bytes) {
   h->arena = nullptr;
   h->arena_cap = 0;
   const size_t want = bytes + (bytes >> 4) + ((size_t)1 << 20);
-  if (cudaMalloc(&h->arena, want) != cudaSuccess) {
+  if (ej_dev_alloc(&h->arena, want) != cudaSuccess) {
     cudaGetLastError();
     h->arena = nullptr;
     return ej_fail(h, EJ_ERR_NOMEM, "device scratch of %zu bytes could not be allocated", want);
@@ -412,7 +435,7 @@ extern "C" ej_status ej_join_host(ej_handle* h, ej_algo algo, const ej_tuple* R,
     if (h->stage) EJ_CUDA(h, cudaFree(h->stage));
     h->stage = nullptr;
     h->stage_cap = 0;
-    if (cudaMalloc(&h->stage, p.bytes) != cudaSuccess) {
+    if (ej_dev_alloc(&h->stage, p.bytes) != cudaSuccess) {
       cudaGetLastError();
       return ej_fail(h, EJ_ERR_NOMEM, "host-path staging of %zu bytes could not be allocated", p.bytes);
     }
@@ -508,7 +531,7 @@ extern "C" ej_status ej_generate(ej_handle* h, const ej_gen_spec* spec, ej_tuple
       EJ_CUDA(h, cudaStreamSynchronize(h->stream));
       cudaFree(h->zipf.d_cdf);
       h->zipf.d_cdf = nullptr;
-      EJ_CUDA(h, cudaMalloc(&h->zipf.d_cdf, sizeof(double) * sp.domain));
+      EJ_CUDA(h, ej_dev_alloc(&h->zipf.d_cdf, sizeof(double) * sp.domain));
       EJ_CUDA(h, cudaMemcpy(h->zipf.d_cdf, cdf.data(), sizeof(double) * sp.domain, cudaMemcpyHostToDevice));
       h->zipf.s = sp.zipf_s;
       h->zipf.domain = sp.domain;

@@ -250,8 +250,8 @@ extern "C" ej_status ej_batch_hash_join(ej_handle* h, const ej_join_desc* joins,
     h->d_batch_counts = nullptr;
     h->h_batch_counts = nullptr;
     h->batch_counts_cap = 0;
-    EJ_CUDA(h, cudaMalloc(&h->d_batch_counts, njoins * sizeof(unsigned long long)));
-    EJ_CUDA(h, cudaMallocHost(&h->h_batch_counts, njoins * sizeof(unsigned long long)));
+    EJ_CUDA(h, ej_dev_alloc(&h->d_batch_counts, njoins * sizeof(unsigned long long)));
+    EJ_CUDA(h, ej_host_alloc(&h->h_batch_counts, njoins * sizeof(unsigned long long)));
     h->batch_counts_cap = njoins;
   }
   EJ_TRY(batch_run(h, joins, njoins, h->d_batch_counts));

@@ -18,8 +18,9 @@
 //     takes its output slot from an atomic cursor (count-only mode sums
 //     per-thread counters instead).  Result order is not deterministic; the
 //     result multiset is.
-// Waits on the mbarrier are bounded by EJ_WAIT_LIMIT_NS and report
-// EJ_ERR_TIMEOUT instead of hanging.
+// Waits on the mbarrier are bounded by the handle's wait limit and report
+// EJ_ERR_TIMEOUT instead of hanging; a CTA that gave up still waits (bounded
+// by EJ_DEFAULT_WAIT_LIMIT_NS) for its own copies in flight before it exits.
 #include "ej_device.cuh"
 #include "ej_entry.h"
 
@@ -50,11 +51,13 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+// non-blocking test of the phase (test_wait returns at once; try_wait may
+// suspend the thread for a time of the hardware's choosing)
+__device__ __forceinline__ bool mbar_test_wait(unsigned long long* bar, unsigned parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity)
@@ -70,11 +73,13 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
       : "memory");
 }
 
-// bounded wait by one thread; true when the phase completed in time
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+// bounded wait by one thread; true when the phase completed in time (limit
+// 0: only if it had completed at the first test)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  unsigned long long limit_ns) {
   const unsigned long long t0 = ej_globaltimer();
-  while (!mbar_try_wait(bar, parity)) {
-    if (ej_globaltimer() - t0 > EJ_WAIT_LIMIT_NS) return false;
+  while (!mbar_test_wait(bar, parity)) {
+    if (ej_globaltimer() - t0 >= limit_ns) return false;
   }
   return true;
 }
@@ -103,7 +108,7 @@ template <bool USE_TMA, bool COUNT_ONLY>
 __global__ void __launch_bounds__(BN_THREADS)
 bnl_kernel(const ej_tuple* __restrict__ R, uint64_t nR, const ej_tuple* __restrict__ S, uint64_t nS,
            uint64_t s_per_cta, ej_result* __restrict__ out, uint64_t cap, unsigned long long* cursor,
-           ej_dev_status* st) {
+           ej_dev_status* st, unsigned long long wait_ns) {
   extern __shared__ __align__(128) unsigned char bn_smem_raw[];
   BnSmem& sm = *reinterpret_cast<BnSmem*>(bn_smem_raw);
 
@@ -149,7 +154,8 @@ bnl_kernel(const ej_tuple* __restrict__ R, uint64_t nR, const ej_tuple* __restri
       issue_tile<USE_TMA>(sm, buf ^ 1, S, t1, (uint32_t)min((uint64_t)BN_STILE, s_end - t1));
     }
     if (USE_TMA) {
-      if (threadIdx.x == 0 && !mbar_wait_bounded(&sm.bar[buf], (unsigned)((t >> 1) & 1u))) sm.timed_out = 1;
+      if (threadIdx.x == 0 && !mbar_wait_bounded(&sm.bar[buf], (unsigned)((t >> 1) & 1u), wait_ns))
+        sm.timed_out = 1;
     }
     __syncthreads();
     if (sm.timed_out) break;
@@ -193,7 +199,8 @@ bnl_kernel(const ej_tuple* __restrict__ R, uint64_t nR, const ej_tuple* __restri
   if (sm.timed_out && threadIdx.x == 0) {
     ej_set_status(st, EJ_ERR_TIMEOUT, 2u);
     // drain copies still in flight so none lands after the CTA exits
-    for (uint64_t u = t; u < ntiles && u <= t + 1; u++) mbar_wait_bounded(&sm.bar[u & 1], (unsigned)((u >> 1) & 1u));
+    for (uint64_t u = t; u < ntiles && u <= t + 1; u++)
+      mbar_wait_bounded(&sm.bar[u & 1], (unsigned)((u >> 1) & 1u), EJ_DEFAULT_WAIT_LIMIT_NS);
   }
   if (COUNT_ONLY) {
     unsigned long long total;
@@ -207,7 +214,8 @@ ej_status launch_bnl(ej_handle* h, dim3 grid, const ej_tuple* R, uint64_t nR, co
                      uint64_t s_per_cta, ej_result* out, uint64_t cap, unsigned long long* cursor) {
   auto k = bnl_kernel<USE_TMA, COUNT_ONLY>;
   EJ_CUDA(h, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BnSmem)));
-  k<<<grid, BN_THREADS, sizeof(BnSmem), h->stream>>>(R, nR, S, nS, s_per_cta, out, cap, cursor, h->d_status);
+  k<<<grid, BN_THREADS, sizeof(BnSmem), h->stream>>>(R, nR, S, nS, s_per_cta, out, cap, cursor, h->d_status,
+                                                      h->wait_limit_ns);
   return ej_check_launch(h, "bnl_kernel");
 }
 

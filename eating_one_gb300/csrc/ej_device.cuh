@@ -8,11 +8,9 @@
 
 #define EJ_FULL_MASK 0xFFFFFFFFu
 
-// Bounded device waits give up after this many nanoseconds of %globaltimer
-// and report EJ_ERR_TIMEOUT through the status word instead of hanging.
-#ifndef EJ_WAIT_LIMIT_NS
-#define EJ_WAIT_LIMIT_NS 1000000000ull
-#endif
+// Bounded device waits give up after a limit in nanoseconds of %globaltimer
+// (the handle's, EJ_DEFAULT_WAIT_LIMIT_NS unless set) and report
+// EJ_ERR_TIMEOUT through the status word instead of hanging.
 
 // 32-bit finaliser of MurmurHash3 (Appleby, public domain): a bijection on
 // uint32, so distinct keys keep distinct hashes and buckets/partitions are
@@ -131,16 +129,22 @@ __device__ __forceinline__ void ej_lookback_publish(unsigned long long* status, 
 
 // ...then walk back over the predecessors (32 per step, one per lane) until
 // one with an inclusive prefix, publish this tile's inclusive prefix and
-// return its exclusive one.  A wait longer than EJ_WAIT_LIMIT_NS takes the
-// missing predecessors as zero and records EJ_ERR_TIMEOUT at `where`.
+// return its exclusive one.  A wait longer than limit_ns takes the missing
+// predecessors as zero and records EJ_ERR_TIMEOUT at `where`; prefixes then
+// come out too small, never too large, so positions derived from them stay
+// inside their buffers.  The clock is read every 64 polls, every poll when
+// the limit is under 100 us (limit 0: give up at the first poll that finds a
+// predecessor not ready).
 __device__ __forceinline__ unsigned long long ej_lookback_resolve(unsigned long long* status, uint64_t tile,
                                                                   unsigned long long aggregate,
-                                                                  ej_dev_status* st, unsigned int where) {
+                                                                  ej_dev_status* st, unsigned int where,
+                                                                  unsigned long long limit_ns) {
   const unsigned int lane = threadIdx.x & 31u;
   if (tile == 0) return 0ull;
   unsigned long long exclusive = 0;
   int64_t k = (int64_t)tile - 1;
   const unsigned long long t0 = ej_globaltimer();
+  const unsigned int period = limit_ns < 100000ull ? 0u : 63u;
   bool gave_up = false;
   for (;;) {
     const int64_t idx = k - (int64_t)lane;
@@ -153,7 +157,7 @@ __device__ __forceinline__ unsigned long long ej_lookback_resolve(unsigned long 
       }
       spins++;
       bool late = false;
-      if ((spins & 63u) == 0u) late = (ej_globaltimer() - t0) > EJ_WAIT_LIMIT_NS;
+      if ((spins & period) == 0u) late = (ej_globaltimer() - t0) >= limit_ns;
       if (__shfl_sync(EJ_FULL_MASK, late ? 1 : 0, 0)) {
         gave_up = true;
         if ((w >> 62) == 0ull) w = (EJ_LB_PREFIX << 62);
@@ -179,7 +183,8 @@ __device__ __forceinline__ unsigned long long ej_lookback_resolve(unsigned long 
 // both halves at once
 __device__ __forceinline__ unsigned long long ej_lookback_warp(unsigned long long* status, uint64_t tile,
                                                              unsigned long long aggregate,
-                                                             ej_dev_status* st, unsigned int where) {
+                                                             ej_dev_status* st, unsigned int where,
+                                                             unsigned long long limit_ns) {
   ej_lookback_publish(status, tile, aggregate);
-  return ej_lookback_resolve(status, tile, aggregate, st, where);
+  return ej_lookback_resolve(status, tile, aggregate, st, where, limit_ns);
 }

@@ -9,6 +9,12 @@
 
 #include "ej.h"
 
+// Bounded device waits (decoupled look-back, mbarrier waits) give up after
+// this many nanoseconds unless the handle sets another limit
+// (EJ_OPT_WAIT_LIMIT_NS); a kernel draining its own copies in flight after
+// giving up always allows this long.
+constexpr unsigned long long EJ_DEFAULT_WAIT_LIMIT_NS = 1000000000ull;
+
 // Device status word: the first error a kernel records wins (atomicCAS on code).
 struct ej_dev_status {
   unsigned int code;  // ej_status
@@ -70,6 +76,8 @@ struct ej_handle {
   ej_prepared_join* prep = nullptr;
   bool prep_valid = false;
   bool opt_count_reuse = true;
+  // bound of every device-side wait of this handle's kernels (EJ_OPT_WAIT_LIMIT_NS)
+  unsigned long long wait_limit_ns = EJ_DEFAULT_WAIT_LIMIT_NS;
 };
 
 // Arena layout: callers first add every buffer to a plan, then reserve once.
@@ -81,6 +89,34 @@ struct ej_plan_bytes {
     return off;
   }
 };
+
+// Every device and pinned-host allocation of the library goes through these,
+// so that ej_inject_alloc_failures can make them fail (api.cu).
+bool ej_alloc_failure_injected();
+template <class T>
+inline cudaError_t ej_dev_alloc(T** p, size_t bytes) {
+  if (ej_alloc_failure_injected()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(reinterpret_cast<void**>(p), bytes);
+}
+template <class T>
+inline cudaError_t ej_host_alloc(T** p, size_t bytes) {
+  if (ej_alloc_failure_injected()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocHost(reinterpret_cast<void**>(p), bytes);
+}
+template <class T>
+inline cudaError_t ej_pool_alloc(T** p, size_t bytes, cudaMemPool_t pool, cudaStream_t s) {
+  if (ej_alloc_failure_injected()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), bytes, pool, s);
+}
 
 ej_status ej_fail(ej_handle* h, ej_status s, const char* fmt, ...);
 // frees the chunked-join resources (stream_join.cu); safe on a handle without them

@@ -93,9 +93,9 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
   const size_t col = ej_table_col_bytes(nR), aux_bytes = ej_table_aux_bytes(tp);
   cudaMemPool_t pool;
   if (index_pool(h->device, &pool) != cudaSuccess ||
-      cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ix->rkey), col, pool, h->stream) != cudaSuccess ||
-      cudaMallocFromPoolAsync(reinterpret_cast<void**>(&ix->rval), col, pool, h->stream) != cudaSuccess ||
-      cudaMallocFromPoolAsync(&ix->aux, aux_bytes, pool, h->stream) != cudaSuccess) {
+      ej_pool_alloc(reinterpret_cast<void**>(&ix->rkey), col, pool, h->stream) != cudaSuccess ||
+      ej_pool_alloc(reinterpret_cast<void**>(&ix->rval), col, pool, h->stream) != cudaSuccess ||
+      ej_pool_alloc(&ix->aux, aux_bytes, pool, h->stream) != cudaSuccess) {
     cudaGetLastError();
     index_release(ix, h->stream);
     return ej_fail(h, EJ_ERR_NOMEM, "index storage of %zu bytes could not be allocated", 2 * col + aux_bytes);

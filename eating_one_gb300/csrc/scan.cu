@@ -19,7 +19,7 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 template <typename In, typename Out>
 __global__ void __launch_bounds__(SCAN_THREADS)
 scan_kernel(const In* __restrict__ in, uint64_t n, Out* __restrict__ out, unsigned long long* status,
-            unsigned int* tile_ctr, uint64_t ntiles, ej_dev_status* st) {
+            unsigned int* tile_ctr, uint64_t ntiles, ej_dev_status* st, unsigned long long wait_ns) {
   __shared__ Out sbuf[SCAN_TILE + SCAN_TILE / 32];
   __shared__ Out warp_tmp[SCAN_THREADS / 32 + 1];
   __shared__ unsigned int s_tile;
@@ -51,7 +51,7 @@ scan_kernel(const In* __restrict__ in, uint64_t n, Out* __restrict__ out, unsign
 
   if (threadIdx.x < 32) {
     const unsigned long long ex =
-        ej_lookback_warp(status, tile, (unsigned long long)aggregate, st, /*where=*/1u);
+        ej_lookback_warp(status, tile, (unsigned long long)aggregate, st, /*where=*/1u, wait_ns);
     if (threadIdx.x == 0) s_prefix = (Out)ex;
   }
   __syncthreads();
@@ -85,7 +85,7 @@ ej_status launch_scan(ej_handle* h, const In* in, uint64_t n, Out* out, void* sc
   unsigned int* ctr = reinterpret_cast<unsigned int*>(status + ntiles);
   EJ_CUDA(h, cudaMemsetAsync(scratch, 0, ntiles * sizeof(unsigned long long) + 16, h->stream));
   scan_kernel<In, Out><<<(unsigned)ntiles, SCAN_THREADS, 0, h->stream>>>(in, n, out, status, ctr, ntiles,
-                                                                         h->d_status);
+                                                                         h->d_status, h->wait_limit_ns);
   return ej_check_launch(h, "scan_kernel");
 }
 
@@ -184,8 +184,8 @@ extern "C" ej_status ej_exclusive_scan_u32_noalloc(const uint32_t* in, uint64_t 
     return EJ_ERR_CUDA;
   }
   unsigned int* ctr = reinterpret_cast<unsigned int*>(d.scratch + ntiles);
-  scan_kernel<uint32_t, unsigned long long><<<(unsigned)ntiles, SCAN_THREADS, 0, s>>>(in, n, o, d.scratch, ctr,
-                                                                                     ntiles, d.status);
+  scan_kernel<uint32_t, unsigned long long><<<(unsigned)ntiles, SCAN_THREADS, 0, s>>>(
+      in, n, o, d.scratch, ctr, ntiles, d.status, EJ_DEFAULT_WAIT_LIMIT_NS);
   if (cudaGetLastError() != cudaSuccess) return EJ_ERR_CUDA;
   ej_dev_status host_status;
   if (cudaMemcpyAsync(&host_status, d.status, sizeof(host_status), cudaMemcpyDeviceToHost, s) != cudaSuccess ||

@@ -205,8 +205,8 @@ extern "C" ej_status ej_server_create(const ej_server_config* cfg, ej_server** o
       return st;
     }
     if (cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&L->d_counts, per_lane * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMallocHost(&L->h_counts, per_lane * sizeof(unsigned long long)) != cudaSuccess) {
+        ej_dev_alloc(&L->d_counts, per_lane * sizeof(unsigned long long)) != cudaSuccess ||
+        ej_host_alloc(&L->h_counts, per_lane * sizeof(unsigned long long)) != cudaSuccess) {
       cudaGetLastError();
       server_free(S);
       return EJ_ERR_NOMEM;
@@ -228,6 +228,7 @@ extern "C" ej_status ej_server_submit(ej_server* srv, const ej_join_desc* join, 
   {
     std::lock_guard<std::mutex> lock(S->mu);
     if (S->stop) return EJ_ERR_BUSY;
+    if (S->cfg.max_queued && S->queue.size() >= S->cfg.max_queued) return EJ_ERR_BUSY;  // admission refused
     S->queue.push_back({*join, tag, arrival_ns ? arrival_ns : ej_now_ns()});
     S->submitted++;
   }

@@ -118,7 +118,7 @@ ej_status sj_device(ej_handle* h, ej_stream_res* r, size_t bytes) {
   EJ_CUDA(h, cudaFree(r->dev));
   r->dev = nullptr;
   r->dev_cap = 0;
-  if (cudaMalloc(&r->dev, bytes) != cudaSuccess) {
+  if (ej_dev_alloc(&r->dev, bytes) != cudaSuccess) {
     (void)cudaGetLastError();
     return ej_fail(h, EJ_ERR_NOMEM, "chunk buffers of %zu bytes could not be allocated", bytes);
   }
@@ -133,7 +133,7 @@ ej_status sj_rowbuf(ej_handle* h, ej_stream_res* r, uint64_t rows) {
   EJ_CUDA(h, cudaFree(r->obuf));
   r->obuf = nullptr;
   r->obuf_rows = 0;
-  if (cudaMalloc(&r->obuf, 2 * rows * sizeof(ej_result)) != cudaSuccess) {
+  if (ej_dev_alloc(&r->obuf, 2 * rows * sizeof(ej_result)) != cudaSuccess) {
     (void)cudaGetLastError();
     return ej_fail(h, EJ_ERR_NOMEM, "row buffers of %llu rows could not be allocated", (unsigned long long)rows);
   }
@@ -144,7 +144,7 @@ ej_status sj_rowbuf(ej_handle* h, ej_stream_res* r, uint64_t rows) {
 ej_status sj_bounce(ej_handle* h, ej_stream_res* r) {
   if (r->pin_cap) return EJ_OK;
   for (int i = 0; i < 2; i++)
-    if (cudaHostAlloc(&r->pin[i], SJ_BOUNCE, cudaHostAllocDefault) != cudaSuccess) {
+    if (ej_host_alloc(&r->pin[i], SJ_BOUNCE) != cudaSuccess) {
       (void)cudaGetLastError();
       return ej_fail(h, EJ_ERR_NOMEM, "pinned bounce buffer of %zu bytes", SJ_BOUNCE);
     }

@@ -73,7 +73,7 @@ struct Pinned {
 
 ej_status tf_pinned(ej_handle* h, Pinned& pin) {
   for (int i = 0; i < 2; i++) {
-    if (cudaHostAlloc(&pin.p[i], TF_CHUNK, cudaHostAllocDefault) != cudaSuccess) {
+    if (ej_host_alloc(&pin.p[i], TF_CHUNK) != cudaSuccess) {
       (void)cudaGetLastError();
       return ej_fail(h, EJ_ERR_NOMEM, "pinned staging buffer of %zu bytes", TF_CHUNK);
     }

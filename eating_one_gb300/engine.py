@@ -94,7 +94,7 @@ class Engine:
         self.lib.ej_set_stream(self.h, torch.cuda.current_stream(self.device).cuda_stream)
 
     def set_option(self, name: str, value: int) -> None:
-        opt = {"partition_bits": 0, "bucket_bits_delta": 1}[name]
+        opt = {"partition_bits": 0, "bucket_bits_delta": 1, "wait_limit_ns": 2, "count_reuse": 3}[name]
         self._check(self.lib.ej_set_option(self.h, opt, value))
 
     def set_timing(self, enable: bool) -> None:

@@ -82,7 +82,7 @@ class ServerConfig(C.Structure):
     """Mirror of ej_server_config (include/ej.h)."""
 
     _fields_ = [("device", C.c_int), ("mode", C.c_int), ("lanes", C.c_uint32), ("max_batch_joins", C.c_uint32),
-                ("lane_bytes", C.c_uint64)]
+                ("lane_bytes", C.c_uint64), ("max_queued", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class Completion(C.Structure):
@@ -151,6 +151,7 @@ _SIGS = {
     "ej_server_drain": [_vp],
     "ej_server_destroy": [_vp],
     "ej_now_ns": [],
+    "ej_inject_alloc_failures": [C.c_uint32],
     "ej_join_host": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_join_host_chunked": [_vp, _i32, _vp, _u64, _vp, _u64, _vp, _u64, _pu64, _vp],
     "ej_exclusive_scan_u32": [_vp, _vp, _u64, _vp],

@@ -25,9 +25,9 @@ BATCHED, PER_JOIN = native.EJ_SERVE_BATCHED, native.EJ_SERVE_PER_JOIN
 
 class Server:
     def __init__(self, mode: int, device: int = 0, lanes: int = 2, max_batch_joins: int = 1024,
-                 lane_bytes: int = 16 << 30):
+                 lane_bytes: int = 16 << 30, max_queued: int = 0):
         self.lib = native.load()
-        cfg = native.ServerConfig(device, mode, lanes, max_batch_joins, lane_bytes)
+        cfg = native.ServerConfig(device, mode, lanes, max_batch_joins, lane_bytes, max_queued, 0)
         h = C.c_void_p()
         st = self.lib.ej_server_create(C.byref(cfg), C.byref(h))
         if st != native.EJ_OK:

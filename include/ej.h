@@ -123,8 +123,19 @@ uint64_t ej_kernel_launches(const ej_handle* h);
 typedef enum ej_option {
   EJ_OPT_PROBE_PARTITION_BITS = 0, /* radix bits of the one S partition pass, 0..8 (0 = probe
                                       in place); -1 (default) lets the planner choose */
-  EJ_OPT_BUCKET_BITS_DELTA = 1     /* hash-table buckets = 2^(ceil(log2|R|) - 2 + delta),
+  EJ_OPT_BUCKET_BITS_DELTA = 1,    /* hash-table buckets = 2^(ceil(log2|R|) - 2 + delta),
                                       delta in -3..3, default 0 */
+  EJ_OPT_WAIT_LIMIT_NS = 2,        /* bound of every device-side wait of this handle's kernels
+                                      (look-back scans, the nested loop's copy waits), in ns,
+                                      0..10^10; -1 restores the default of 10^9 (1 s).  A wait
+                                      that runs out makes the call return EJ_ERR_TIMEOUT (its
+                                      results are then not valid); the handle stays usable.
+                                      0 gives up at the first poll that finds a wait unmet, which
+                                      lets tests drive the timeout path without a hung kernel */
+  EJ_OPT_COUNT_REUSE = 3           /* 1 (default): ej_hash_join_count keeps its table, partitioned
+                                      S and run descriptors for an ej_hash_join that follows on the
+                                      same relations; 0: the count keeps nothing (and writes no
+                                      run descriptors) */
 } ej_option;
 ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value);
 
@@ -148,7 +159,15 @@ ej_status ej_set_tuning(ej_handle* h, const ej_tune_entry* entries, uint32_t n);
  * partitioning.cu:15-271, countPartition :273-293, count/join join_gpu.cu:9-113). */
 ej_status ej_hash_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S, uint64_t nS,
                        ej_result* out, uint64_t out_cap, uint64_t* out_count);
-/* count pass only (join_gpu.cu:9-66 + presum + getValue, hj.cc:997-1048) */
+/* Count pass only (join_gpu.cu:9-66 + presum + getValue, hj.cc:997-1048).
+ * The reference sizes its output this way and then joins (hj.cc:997-1115);
+ * to make that sequence one build, the count keeps its R table, its
+ * partitioned copy of S and every probe's run descriptor in the handle, and
+ * an ej_hash_join (or ej_hash_join_async) that follows it on the same handle
+ * with the same R, nR, S and nS only writes the rows from them.  R and S must
+ * not change in between.  Any other call that uses the handle's scratch drops
+ * what the count kept (the join then runs whole); a write cut short by
+ * out_cap keeps it for the retry.  EJ_OPT_COUNT_REUSE = 0 turns this off. */
 ej_status ej_hash_join_count(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
                              uint64_t nS, uint64_t* out_count);
 /* Asynchronous form: no host synchronisation; the total count is written to
@@ -278,6 +297,9 @@ typedef struct ej_server_config {
   uint32_t max_batch_joins; /* joins per batch (0: 1024); 1 in EJ_SERVE_PER_JOIN */
   uint64_t lane_bytes;      /* device scratch budget per lane (0: 16 GiB); a single
                                larger request still runs, alone */
+  uint32_t max_queued;      /* requests waiting for a lane at once (0: no limit); a
+                               submit past it is refused with EJ_ERR_BUSY */
+  uint32_t reserved;        /* 0 */
 } ej_server_config;
 
 typedef struct ej_completion {
@@ -293,7 +315,9 @@ typedef struct ej_completion {
 typedef struct ej_server ej_server;
 
 ej_status ej_server_create(const ej_server_config* cfg, ej_server** out);
-/* Queue one request (thread-safe).  arrival_ns = 0 stamps the current time. */
+/* Queue one request (thread-safe).  arrival_ns = 0 stamps the current time.
+ * EJ_ERR_BUSY: refused (max_queued requests already wait, or the server is
+ * shutting down); the request was not queued and never completes. */
 ej_status ej_server_submit(ej_server* s, const ej_join_desc* join, uint64_t tag, uint64_t arrival_ns);
 /* Take up to max completions; waits up to wait_us microseconds for the first. */
 ej_status ej_server_poll(ej_server* s, ej_completion* out, uint32_t max, uint32_t* n, uint32_t wait_us);
@@ -350,14 +374,25 @@ ej_status ej_exclusive_scan_u32(ej_handle* h, const uint32_t* in, uint64_t n, ui
  * EJ_NOALLOC_SCAN_MAX_N inputs (about 512 KB, held on every device that loads
  * the library until the process exits); larger n returns EJ_ERR_TOO_LARGE.
  * in and out (n + 1 uint64 offsets, out[n] = total) are device pointers owned
- * by the caller; the scan runs on `stream` on the current device and the call
- * returns after it has finished.  The first call on a device looks up the
+ * by the caller; the scan runs on `stream` on the current device, and every
+ * call synchronises `stream` before it returns (it reads the scan's status
+ * word back to the host).  The first call on a device looks up the
  * scratch address for that device; make that first call before any stream
  * capture.  All calls share the one scratch array, so calls that overlap on
  * the GPU (other streams or host threads) race and must be serialised by the
  * caller. */
 #define EJ_NOALLOC_SCAN_MAX_N (1ull << 28)
 ej_status ej_exclusive_scan_u32_noalloc(const uint32_t* in, uint64_t n, uint64_t* out, ej_stream stream);
+
+/* ---- failure injection for tests ------------------------------------------- */
+
+/* The next `count` device or pinned-host allocations the library makes (any
+ * handle, index, server or host-buffer path, any thread) fail as if the memory
+ * were exhausted, so that a caller's handling of EJ_ERR_NOMEM can be tested
+ * without exhausting a shared GPU's memory.  0 clears it.  The reference has
+ * no counterpart (its drivers exit(1) on any failed cuMemAlloc,
+ * joins/hashJoin_gpu/main_street/hj.cc:467-475). */
+void ej_inject_alloc_failures(uint32_t count);
 
 /* ---- inputs and checks --------------------------------------------------- */
 
