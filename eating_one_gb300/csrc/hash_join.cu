@@ -8,8 +8,10 @@
 // compares per block, and the write pass repeats all of them.
 //
 // Here:
-//   build  R is sorted by hash32(val) with four 8-bit LSD radix passes
-//          (radix.cu); the last pass writes it as two arrays rkey[]/rval[],
+//   build  R is sorted by hash32(val): tables of 2^20 rows and more by two
+//          unordered MSD passes and a shared-memory sort per 16-bit bucket
+//          (msd.cu), smaller ones and sorted indexes by four 8-bit LSD radix
+//          passes (radix.cu); either writes it as two arrays rkey[]/rval[],
 //          and start[b] marks where bucket b (top hb hash bits) begins - the
 //          grouped layout of the reference's hash index (Bucket + Buck_array,
 //          joins/CPU_JOIN/inner_cpu/inner-idx-bnlj.cc:142-166), built on the
@@ -293,7 +295,11 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
   const size_t tuples = (size_t)(nR ? nR : 1) * sizeof(ej_tuple);
   tp.tmp_a_off = p.add(tuples);
   tp.tmp_b_off = p.add(tuples);
-  ej_radix_plan_add(p, tp.rplan, nR);
+  tp.msd = kind == EJ_TABLE_HASH && nR >= EJ_MSD_MIN_ROWS;
+  if (tp.msd)
+    ej_msd_plan_add(p, tp.mplan, nR);
+  else
+    ej_radix_plan_add(p, tp.rplan, nR);
   if (tp.use_dir) {  // directory build scratch
     const uint64_t tiles = (nR + DIR_TILE - 1) / DIR_TILE + 1;
     tp.dir_keys_off = p.add(tiles * sizeof(uint32_t));
@@ -318,7 +324,8 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
   ej_tuple* tmp[2] = {reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.tmp_a_off)),
                       reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.tmp_b_off))};
   const ej_tuple* src = R;
-  for (uint32_t p = 0; p < tp.passes && tp.nR; p++) {
+  if (tp.msd) EJ_TRY(ej_msd_sort(h, tp.mplan, R, tmp[0], tmp[1], rkey, rval));
+  for (uint32_t p = 0; p < tp.passes && tp.nR && !tp.msd; p++) {
     const uint32_t shift = 8u * p;
     if (p + 1 == tp.passes) {
       EJ_TRY(ej_radix_pass_soa(h, tp.rplan, src, rkey, rval, shift, 8u, digit_kind));

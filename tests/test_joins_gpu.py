@@ -211,6 +211,45 @@ def test_count_then_join_writes_from_the_count(engine, pb):
         engine.set_option("partition_bits", -1)
 
 
+@pytest.mark.parametrize("shape", ["three_keys", "hot_keys", "long_runs"])
+def test_msd_table_build_skew(engine, shape):
+    """Tables of 2^20 rows and more are sorted by two MSD passes and one
+    shared-memory sort per 16-bit hash bucket.  Skewed tables take its other
+    paths: buckets too large for shared memory (sorted through global memory:
+    three keys, or hot keys among unique ones), and sub-buckets longer than one
+    thread's insertion sort (runs of 40 to 3000 rows of one key)."""
+    rng = np.random.default_rng({"three_keys": 1, "hot_keys": 2, "long_runs": 3}[shape])
+    n = (1 << 20) + 333
+    if shape == "three_keys":
+        vals = rng.integers(5, 8, n)
+        S = rel(rng, 20, 4, 9, key_base=n)
+    else:
+        vals = rng.choice(1 << 30, size=n, replace=False)
+        if shape == "hot_keys":
+            hot = rng.choice(1 << 30, size=40, replace=False)
+            vals[: n // 5] = hot[rng.integers(0, 40, n // 5)]
+            skewed = vals[: n // 5]
+        else:
+            runs = rng.integers(40, 3000, 60)
+            pos = np.cumsum(np.concatenate([[0], runs]))
+            for i in range(60):
+                vals[pos[i]:pos[i + 1]] = vals[pos[i]]
+            skewed = vals[: pos[-1]]
+        S = np.empty((1 << 18, 2), dtype=np.int32)
+        S[:, 0] = np.arange(n, n + len(S))
+        S[:, 1] = vals[rng.integers(0, n, len(S))]
+        S[: len(S) // 8, 1] = rng.integers(0, 1 << 30, len(S) // 8)
+        # the skewed keys only in S rows 0..7; elsewhere 12345 replaces them
+        # (a key R holds once at most), so the result stays small
+        S[8:, 1] = np.where(np.isin(S[8:, 1], skewed), 12345, S[8:, 1])
+        S[:8, 1] = skewed[:8]
+    R = np.stack([np.arange(n), vals], axis=1).astype(np.int32)
+    R = R[rng.permutation(n)]
+    ref = O.hash_join(R, S)
+    same_multiset(engine.join("hash", dev(R), dev(S)), ref)
+    same_multiset(engine.join("hash_index", dev(R), dev(S)), ref)
+
+
 @pytest.mark.parametrize("n,dup,s_rows", [(1 << 22, 1, 1 << 23), (1 << 22, 3, 1 << 23), (1 << 20, 1, 17 << 20)])
 def test_directory_or_buckets(engine, n, dup, s_rows):
     """A 2^22-row table keeps its key directory when its runs average two rows
