@@ -8,9 +8,11 @@
 //   2. an unordered segmented pass by bits 16..23 inside every segment (65536
 //      buckets of about |R|/65536 rows) - its tile descriptors are laid out on
 //      the device from the first pass's offsets, so the host never waits;
-//   3. one CTA per bucket orders the bucket by bits 0..15 in shared memory
-//      (counting by bits 8..15, then each of the 256 sub-buckets by bits 0..7)
-//      and writes the table's two columns rkey[]/rval[].
+//   3. one CTA per group of consecutive buckets (about 2048 rows) orders the
+//      group by its remaining hash bits in shared memory (a counting pass by
+//      12 of them into sub-buckets of a few rows, then every row ranked within
+//      its sub-bucket) and writes each row once, to its place in the table's
+//      two columns rkey[]/rval[].
 // Three passes over R instead of the four of an LSD sort, none with the
 // ballot ranking a stable pass needs.  A bucket too large for shared memory
 // (many rows of few keys) is sorted by its CTA through global memory
@@ -27,9 +29,13 @@ namespace {
 constexpr uint32_t MSD_BUCKET_BITS = 16;
 constexpr uint32_t MSD_BUCKETS = 1u << MSD_BUCKET_BITS;
 constexpr int LS_THREADS = 256;
-constexpr int LS_CAP = 3072;                 // rows of a bucket sorted in shared memory
+constexpr int LS_CAP = 3072;                 // rows of a bucket group sorted in shared memory
 constexpr int LS_PER = LS_CAP / LS_THREADS;  // rows per thread
-constexpr uint32_t LS_SMALL = 32;            // sub-buckets up to this size: one thread's insertion sort
+constexpr uint32_t LS_ROWS = 2048;           // bucket groups aim at this many rows
+constexpr uint32_t LS_DIGIT_BITS = 12;       // digit of the counting pass in shared memory
+constexpr uint32_t LS_DIGITS = 1u << LS_DIGIT_BITS;
+constexpr uint32_t LS_MAX_GROUP_BITS = 4;    // groups of at most 16 buckets
+constexpr uint32_t LS_SMALL = 32;            // sub-buckets up to this size: each row ranked on its own
 
 // the first pass's digit d (cells d * ntiles1 + t) is segment d: its start,
 // its tiles, and the first tile of the second pass it gets
@@ -111,46 +117,56 @@ __global__ void __launch_bounds__(256) msd_bucket_kernel(const MsdSegments* __re
 }
 
 struct LsSmem {
-  uint2 row[LS_CAP];      // the bucket's tuples in sub-bucket order
-  uint32_t hsh[LS_CAP];   // their hashes
-  uint32_t cnt[256];      // counts of a digit, then running positions
-  uint32_t start[257];    // sub-bucket starts
+  uint2 row[LS_CAP];              // the group's tuples in digit order
+  uint32_t hsh[LS_CAP];           // their hashes
+  uint32_t cnt[LS_DIGITS + 1];    // digit counts, then digit starts (cnt[LS_DIGITS] = rows)
+  uint32_t cnt2[256];             // counts of a long sub-bucket's remaining bits (at most 8 of them)
+  uint32_t big[LS_CAP / (LS_SMALL + 1) + 1];  // digits whose sub-bucket is longer than LS_SMALL
   uint32_t warp_tmp[LS_THREADS / 32 + 1];
   uint32_t nbig;
-  uint32_t big[256];      // sub-buckets longer than LS_SMALL
-  uint8_t isbig[256];
 };
 
-// exclusive sum of cnt[0..255] into dst[0..255] (dst[256] = total); every thread
-__device__ __forceinline__ void ls_scan256(const uint32_t* cnt, uint32_t* dst, uint32_t* warp_tmp) {
-  const uint32_t v = cnt[threadIdx.x];
+// exclusive sum in place of the LS_DIGITS counters c[0..] (c[LS_DIGITS] =
+// total); every thread, LS_DIGITS / LS_THREADS consecutive counters each
+__device__ __forceinline__ void ls_scan_digits(uint32_t* c, uint32_t* warp_tmp) {
+  constexpr int PER = LS_DIGITS / LS_THREADS;
+  uint32_t v[PER], sum = 0;
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    v[i] = c[threadIdx.x * PER + i];
+    sum += v[i];
+  }
   uint32_t total;
-  const uint32_t ex = ej_block_exclusive_sum<LS_THREADS, uint32_t>(v, warp_tmp, &total);
-  dst[threadIdx.x] = ex;
-  if (threadIdx.x == 0) dst[256] = total;
+  uint32_t run = ej_block_exclusive_sum<LS_THREADS, uint32_t>(sum, warp_tmp, &total);
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    c[threadIdx.x * PER + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == 0) c[LS_DIGITS] = total;
   __syncthreads();
 }
 
 // The CTA sorts the rows [a, a + len) of `src` by hash bits 0..7 (all of them
 // share bits 8..31) into rkey/rval at the same positions: a counting sort
 // through global memory (order among equal hashes, which are equal keys,
-// unspecified).  Shared counters: sm.cnt.
+// unspecified).  Shared counters: sm.cnt2.
 __device__ void ls_digit_global(LsSmem& sm, const ej_tuple* __restrict__ src, uint64_t a, uint32_t len,
                                 int32_t* __restrict__ rkey, int32_t* __restrict__ rval) {
-  sm.cnt[threadIdx.x] = 0;
+  sm.cnt2[threadIdx.x] = 0;
   __syncthreads();
   const uint2* s2 = reinterpret_cast<const uint2*>(src);
   for (uint32_t j = threadIdx.x; j < len; j += LS_THREADS)
-    atomicAdd(&sm.cnt[ej_hash32(s2[a + j].y) & 255u], 1u);
+    atomicAdd(&sm.cnt2[ej_hash32(s2[a + j].y) & 255u], 1u);
   __syncthreads();
-  uint32_t c = sm.cnt[threadIdx.x];
+  uint32_t c = sm.cnt2[threadIdx.x];
   uint32_t total;
   const uint32_t ex = ej_block_exclusive_sum<LS_THREADS, uint32_t>(c, sm.warp_tmp, &total);
-  sm.cnt[threadIdx.x] = ex;
+  sm.cnt2[threadIdx.x] = ex;
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < len; j += LS_THREADS) {
     const uint2 x = s2[a + j];
-    const uint32_t p = atomicAdd(&sm.cnt[ej_hash32(x.y) & 255u], 1u);
+    const uint32_t p = atomicAdd(&sm.cnt2[ej_hash32(x.y) & 255u], 1u);
     rkey[a + p] = (int32_t)x.x;
     rval[a + p] = (int32_t)x.y;
   }
@@ -159,128 +175,151 @@ __device__ void ls_digit_global(LsSmem& sm, const ej_tuple* __restrict__ src, ui
 
 // A bucket larger than shared memory: by bits 8..15 from `in` into `tmp`
 // (same positions), then every sub-bucket by bits 0..7 into the columns.
+// Shared counters: sm.cnt (256 of them, with their starts in cnt[256 ...]).
 __device__ void ls_bucket_global(LsSmem& sm, const ej_tuple* __restrict__ in, ej_tuple* __restrict__ tmp,
                                  uint64_t lo, uint32_t m, int32_t* __restrict__ rkey, int32_t* __restrict__ rval) {
   const uint2* s2 = reinterpret_cast<const uint2*>(in);
   uint2* t2 = reinterpret_cast<uint2*>(tmp);
-  sm.cnt[threadIdx.x] = 0;
+  uint32_t* cur = sm.cnt;
+  uint32_t* st = sm.cnt + 256;  // 257 starts
+  cur[threadIdx.x] = 0;
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < m; j += LS_THREADS) atomicAdd(&sm.cnt[(ej_hash32(s2[lo + j].y) >> 8) & 255u], 1u);
+  for (uint32_t j = threadIdx.x; j < m; j += LS_THREADS) atomicAdd(&cur[(ej_hash32(s2[lo + j].y) >> 8) & 255u], 1u);
   __syncthreads();
-  ls_scan256(sm.cnt, sm.start, sm.warp_tmp);
-  sm.cnt[threadIdx.x] = sm.start[threadIdx.x];
-  __syncthreads();
+  {
+    const uint32_t c = cur[threadIdx.x];
+    uint32_t total;
+    const uint32_t ex = ej_block_exclusive_sum<LS_THREADS, uint32_t>(c, sm.warp_tmp, &total);
+    st[threadIdx.x] = ex;
+    cur[threadIdx.x] = ex;
+    if (threadIdx.x == 0) st[256] = total;
+    __syncthreads();
+  }
   for (uint32_t j = threadIdx.x; j < m; j += LS_THREADS) {
     const uint2 x = s2[lo + j];
-    const uint32_t p = atomicAdd(&sm.cnt[(ej_hash32(x.y) >> 8) & 255u], 1u);
+    const uint32_t p = atomicAdd(&cur[(ej_hash32(x.y) >> 8) & 255u], 1u);
     t2[lo + p] = x;
   }
   __syncthreads();  // the CTA's own global writes are visible to it past the barrier
   for (uint32_t s = 0; s < 256; s++) {
-    const uint32_t a = sm.start[s], len = sm.start[s + 1] - a;
+    const uint32_t a = st[s], len = st[s + 1] - a;
     if (len) ls_digit_global(sm, tmp, lo + a, len, rkey, rval);
   }
 }
 
-// One CTA per bucket b = top 16 hash bits: rows [bstart[b], bstart[b + 1]) of
-// `in` (ordered by those bits) into the columns, ordered by the full hash.
-__global__ void __launch_bounds__(LS_THREADS)
-msd_local_kernel(const ej_tuple* __restrict__ in, ej_tuple* __restrict__ tmp, const uint32_t* __restrict__ bstart,
-                 int32_t* __restrict__ rkey, int32_t* __restrict__ rval) {
-  extern __shared__ __align__(16) unsigned char ls_smem_raw[];
-  LsSmem& sm = *reinterpret_cast<LsSmem*>(ls_smem_raw);
-  const uint32_t b = blockIdx.x;
-  // bounds clamped to [0, n) and ordered (they are, unless a scan timed out)
-  const uint32_t n = bstart[MSD_BUCKETS];
-  const uint64_t lo = min(bstart[b], n);
-  const uint32_t m = max(min(bstart[b + 1], n), (uint32_t)lo) - (uint32_t)lo;
-  if (m == 0) return;
-  if (m > (uint32_t)LS_CAP) {
-    ls_bucket_global(sm, in, tmp, lo, m, rkey, rval);
-    return;
-  }
+// The CTA sorts the m <= LS_CAP rows [lo, lo + m) of `in`, which share hash
+// bits low_bits..31 (LS_DIGIT_BITS <= low_bits <= LS_DIGIT_BITS + 8), into the
+// columns by the full hash: a counting pass by the LS_DIGIT_BITS bits below
+// low_bits groups the rows into sub-buckets of a few rows each; every row's
+// place in its sub-bucket is the number of rows there with a smaller hash
+// (or the same hash and an earlier slot), so each row is written once, at
+// its final position.  Long sub-buckets (many rows of few keys) are sorted
+// by the whole CTA instead: a counting sort by their remaining bits.
+__device__ void ls_sort_smem(LsSmem& sm, const ej_tuple* __restrict__ in, uint64_t lo, uint32_t m,
+                             uint32_t low_bits, int32_t* __restrict__ rkey, int32_t* __restrict__ rval) {
   const unsigned t = threadIdx.x;
-  sm.cnt[t] = 0;
-  sm.isbig[t] = 0;
+  const uint32_t sh = low_bits - LS_DIGIT_BITS;  // bits under the digit
+  for (uint32_t i = t; i < LS_DIGITS; i += LS_THREADS) sm.cnt[i] = 0;
   if (t == 0) sm.nbig = 0;
   __syncthreads();
-  // 1. rows into registers (coalesced), ranked within their bits 8..15 digit
+  // 1. rows into registers (coalesced), ranked within their digit
   const uint2* src = reinterpret_cast<const uint2*>(in) + lo;
   uint2 v[LS_PER];
-  uint32_t h[LS_PER], rk[LS_PER];
+  uint32_t rk[LS_PER];
 #pragma unroll
   for (int i = 0; i < LS_PER; i++) {
     const uint32_t j = t + (uint32_t)i * LS_THREADS;
-    if (j < m) {
-      v[i] = __ldcs(src + j);
-      h[i] = ej_hash32(v[i].y);
-    }
+    if (j < m) v[i] = __ldcs(src + j);
   }
 #pragma unroll
   for (int i = 0; i < LS_PER; i++)
-    if (t + (uint32_t)i * LS_THREADS < m) rk[i] = atomicAdd(&sm.cnt[(h[i] >> 8) & 255u], 1u);
+    if (t + (uint32_t)i * LS_THREADS < m)
+      rk[i] = atomicAdd(&sm.cnt[(ej_hash32(v[i].y) >> sh) & (LS_DIGITS - 1)], 1u);
   __syncthreads();
-  ls_scan256(sm.cnt, sm.start, sm.warp_tmp);
-  // 2. every row to its sub-bucket
+  ls_scan_digits(sm.cnt, sm.warp_tmp);
+  // 2. every row to its digit's sub-bucket
 #pragma unroll
   for (int i = 0; i < LS_PER; i++)
     if (t + (uint32_t)i * LS_THREADS < m) {
-      const uint32_t p = sm.start[(h[i] >> 8) & 255u] + rk[i];
+      const uint32_t hv = ej_hash32(v[i].y);
+      const uint32_t p = sm.cnt[(hv >> sh) & (LS_DIGITS - 1)] + rk[i];
       sm.row[p] = v[i];
-      sm.hsh[p] = h[i];
+      sm.hsh[p] = hv;
     }
   __syncthreads();
-  // 3. sub-bucket t by bits 0..7: insertion sort by one thread when short,
-  //    else by the whole CTA below
-  {
-    const uint32_t a = sm.start[t], e = sm.start[t + 1];
-    if (e - a <= LS_SMALL) {
-      for (uint32_t i = a + 1; i < e; i++) {
-        const uint32_t hk = sm.hsh[i];
-        const uint2 rw = sm.row[i];
-        uint32_t j = i;
-        while (j > a && sm.hsh[j - 1] > hk) {
-          sm.hsh[j] = sm.hsh[j - 1];
-          sm.row[j] = sm.row[j - 1];
-          j--;
-        }
-        sm.hsh[j] = hk;
-        sm.row[j] = rw;
-      }
-    } else {
-      sm.big[atomicAdd(&sm.nbig, 1u)] = t;
-      sm.isbig[t] = 1;
+  // 3. each row of a short sub-bucket straight to its place (the lanes of a
+  //    warp take consecutive slots, so their stores stay within a few rows
+  //    of each other); long sub-buckets are listed for step 4
+  for (uint32_t p = t; p < m; p += LS_THREADS) {
+    const uint32_t hv = sm.hsh[p];
+    const uint32_t d = (hv >> sh) & (LS_DIGITS - 1);
+    const uint32_t a = sm.cnt[d], e = sm.cnt[d + 1];
+    if (e - a > LS_SMALL) {
+      if (p == a) sm.big[atomicAdd(&sm.nbig, 1u)] = d;
+      continue;
     }
+    uint32_t r = a;
+    for (uint32_t q = a; q < e; q++) {
+      const uint32_t x = sm.hsh[q];
+      r += (x < hv || (x == hv && q < p)) ? 1u : 0u;
+    }
+    const uint2 row = sm.row[p];
+    rkey[lo + r] = (int32_t)row.x;
+    rval[lo + r] = (int32_t)row.y;
   }
   __syncthreads();
-  // 4. the rows of short sub-buckets to the columns (coalesced)
-  for (uint32_t k = t; k < m; k += LS_THREADS) {
-    if (sm.isbig[(sm.hsh[k] >> 8) & 255u]) continue;
-    const uint2 x = sm.row[k];
-    rkey[lo + k] = (int32_t)x.x;
-    rval[lo + k] = (int32_t)x.y;
-  }
-  // 5. long sub-buckets: a counting sort by bits 0..7, straight to the columns
-  const uint32_t nbig = sm.nbig;
+  // 4. long sub-buckets: a counting sort by the bits under the digit,
+  //    straight to the columns
+  const uint32_t nbig = sm.nbig, rmask = (1u << sh) - 1u;
   for (uint32_t q = 0; q < nbig; q++) {
-    const uint32_t s = sm.big[q];
-    const uint32_t a = sm.start[s], len = sm.start[s + 1] - a;
+    const uint32_t d = sm.big[q];
+    const uint32_t a = sm.cnt[d], len = sm.cnt[d + 1] - a;
+    sm.cnt2[t] = 0;
     __syncthreads();
-    sm.cnt[t] = 0;
+    for (uint32_t j = t; j < len; j += LS_THREADS) atomicAdd(&sm.cnt2[sm.hsh[a + j] & rmask], 1u);
     __syncthreads();
-    for (uint32_t j = t; j < len; j += LS_THREADS) atomicAdd(&sm.cnt[sm.hsh[a + j] & 255u], 1u);
-    __syncthreads();
-    const uint32_t c = sm.cnt[t];
+    const uint32_t c = sm.cnt2[t];
     uint32_t total;
     const uint32_t ex = ej_block_exclusive_sum<LS_THREADS, uint32_t>(c, sm.warp_tmp, &total);
-    sm.cnt[t] = ex;
+    sm.cnt2[t] = ex;
     __syncthreads();
     for (uint32_t j = t; j < len; j += LS_THREADS) {
-      const uint32_t p = a + atomicAdd(&sm.cnt[sm.hsh[a + j] & 255u], 1u);
       const uint2 x = sm.row[a + j];
+      const uint32_t p = a + atomicAdd(&sm.cnt2[sm.hsh[a + j] & rmask], 1u);
       rkey[lo + p] = (int32_t)x.x;
       rval[lo + p] = (int32_t)x.y;
     }
+    __syncthreads();
+  }
+  __syncthreads();  // shared memory is reused by the caller's next range
+}
+
+// One CTA per group of 2^g consecutive buckets (b = top 16 hash bits), whose
+// rows [bstart[b0], bstart[b0 + 2^g]) of `in` share hash bits 16 + g .. 31:
+// into the columns ordered by the full hash.  A group larger than shared
+// memory goes bucket by bucket, and a bucket larger than shared memory
+// through global memory.
+__global__ void __launch_bounds__(LS_THREADS, 4)
+msd_local_kernel(const ej_tuple* __restrict__ in, ej_tuple* __restrict__ tmp, const uint32_t* __restrict__ bstart,
+                 uint32_t g, int32_t* __restrict__ rkey, int32_t* __restrict__ rval) {
+  extern __shared__ __align__(16) unsigned char ls_smem_raw[];
+  LsSmem& sm = *reinterpret_cast<LsSmem*>(ls_smem_raw);
+  // bounds clamped to [0, n) and ordered (they are, unless a scan timed out)
+  const uint32_t n = bstart[MSD_BUCKETS];
+  const uint32_t b0 = blockIdx.x << g, b1 = b0 + (1u << g);
+  const uint32_t lo = min(bstart[b0], n);
+  const uint32_t hi = max(min(bstart[b1], n), lo);
+  if (hi - lo <= (uint32_t)LS_CAP) {
+    if (hi > lo) ls_sort_smem(sm, in, lo, hi - lo, MSD_BUCKET_BITS + g, rkey, rval);
+    return;
+  }
+  for (uint32_t b = b0; b < b1; b++) {
+    const uint32_t blo = max(min(bstart[b], n), lo);
+    const uint32_t bhi = min(max(min(bstart[b + 1], n), blo), hi);
+    if (bhi - blo > (uint32_t)LS_CAP)
+      ls_bucket_global(sm, in, tmp, blo, bhi - blo, rkey, rval);
+    else if (bhi > blo)
+      ls_sort_smem(sm, in, blo, bhi - blo, MSD_BUCKET_BITS, rkey, rval);
   }
 }
 
@@ -323,7 +362,10 @@ ej_status ej_msd_sort(ej_handle* h, const ej_msd_plan& mp, const ej_tuple* R, ej
   const uint32_t* offs2 = reinterpret_cast<const uint32_t*>(ej_arena_at(h, mp.pass2.offs_off));
   msd_bucket_kernel<<<(MSD_BUCKETS + 1 + 255) / 256, 256, 0, h->stream>>>(seg, offs2, mp.n, bstart);
   EJ_TRY(ej_check_launch(h, "msd_bucket_kernel"));
+  // groups of 2^g buckets of about LS_ROWS rows in all
+  uint32_t g = 0;
+  while (g < LS_MAX_GROUP_BITS && ((uint64_t)LS_ROWS << MSD_BUCKET_BITS) >= (mp.n << (g + 1))) g++;
   EJ_CUDA(h, cudaFuncSetAttribute(msd_local_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LsSmem)));
-  msd_local_kernel<<<MSD_BUCKETS, LS_THREADS, sizeof(LsSmem), h->stream>>>(tmp_b, tmp_a, bstart, rkey, rval);
+  msd_local_kernel<<<MSD_BUCKETS >> g, LS_THREADS, sizeof(LsSmem), h->stream>>>(tmp_b, tmp_a, bstart, g, rkey, rval);
   return ej_check_launch(h, "msd_local_kernel");
 }
