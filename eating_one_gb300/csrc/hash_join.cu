@@ -178,10 +178,10 @@ __device__ __forceinline__ void ej_prefetch_tile(const void* base, uint64_t w, u
   if (lane < 8u && off < nP * 8) asm volatile("prefetch.global.L2 [%0];" ::"l"(static_cast<const char*>(base) + off));
 }
 
-template <int KIND, bool OUTER, bool DESC>
+template <int KIND, bool OUTER, int DESC>
 __global__ void __launch_bounds__(PR_THREADS, 5)  // 40 warps per SM hide the table loads
 probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* __restrict__ wcount,
-                   uint64_t nwtiles, uint2* __restrict__ desc, uint64_t ahead) {
+                   uint64_t nwtiles, void* __restrict__ desc, uint64_t ahead) {
   const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + (threadIdx.x >> 5);
   if (w >= nwtiles) return;
   ej_prefetch_tile(P, w + ahead, nP, threadIdx.x & 31u);  // the tile a warp one resident wave later takes
@@ -189,8 +189,9 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   if ((threadIdx.x & 31u) == 0) wcount[w] = total;
 }
 
+template <int KIND, bool OUTER, int DESC>
 __global__ void __launch_bounds__(PR_THREADS)
-probe_write_kernel(const ej_tuple* __restrict__ P, const uint2* __restrict__ desc, uint64_t nP, ej_table_view t,
+probe_write_kernel(const ej_tuple* __restrict__ P, const void* __restrict__ desc, uint64_t nP, ej_table_view t,
                    const unsigned long long* __restrict__ woff, uint64_t nwtiles, ej_result* __restrict__ out,
                    uint64_t cap, ej_dev_status* st, uint64_t ahead) {
   __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
@@ -199,10 +200,17 @@ probe_write_kernel(const ej_tuple* __restrict__ P, const uint2* __restrict__ des
   if (w >= nwtiles) return;
   if (w == 0 && threadIdx.x == 0 && woff[nwtiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
   ej_prefetch_tile(P, w + ahead, nP, threadIdx.x & 31u);  // the tile a warp one resident wave later takes
-  ej_prefetch_tile(desc, w + ahead, nP, (threadIdx.x & 31u) - 8u);
+  // the tile's descriptors: 1 KB (wide, lanes 8..15) or 512 bytes (packed, lanes 8..11)
+  if (DESC == EJ_DESC_PACKED) {
+    const unsigned l = (threadIdx.x & 31u) - 8u;
+    const uint64_t doff = (w + ahead) * (PR_WTILE * 4) + (uint64_t)l * 128u;
+    if (l < 4u && doff < nP * 4) asm volatile("prefetch.global.L2 [%0];" ::"l"(static_cast<const char*>(desc) + doff));
+  } else {
+    ej_prefetch_tile(desc, w + ahead, nP, (threadIdx.x & 31u) - 8u);
+  }
   const unsigned long long off = woff[w];
   if (off >= cap) return;
-  ej_probe_write_warp(P, desc, w * PR_WTILE, nP, t, off, out, cap, stage[warp]);
+  ej_probe_write_warp<KIND, OUTER, DESC>(P, desc, w * PR_WTILE, nP, t, off, out, cap, stage[warp]);
 }
 
 // One pass (the joins that materialise rows in one call): each warp finds the
@@ -243,18 +251,40 @@ probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   ej_emit_warp(pw, kk, t, off, out, cap, stage[warp]);
 }
 
+// the descriptor form of a table: packed (4 bytes) when its row positions fit
+// in 27 bits, else wide; the count and the write pass of one probe decide it
+// from the same table view
+static int desc_form(const ej_table_view& t) { return t.nR < EJ_PACKED_MAX_ROWS ? EJ_DESC_PACKED : EJ_DESC_WIDE; }
+
 template <int KIND, bool OUTER>
 ej_status launch_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                       unsigned long long* wcount, uint2* desc) {
-  if (desc)
-    probe_count_kernel<KIND, OUTER, true>
-        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, desc,
-                                                            (uint64_t)h->num_sms * 5 * PR_WARPS);
+                       unsigned long long* wcount, void* desc) {
+  const uint64_t ahead = (uint64_t)h->num_sms * 5 * PR_WARPS;
+  const dim3 grid((unsigned)pp.ntiles);
+  if (!desc)
+    probe_count_kernel<KIND, OUTER, EJ_DESC_NONE><<<grid, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount,
+                                                                                      pp.nwtiles, nullptr, ahead);
+  else if (desc_form(t) == EJ_DESC_PACKED)
+    probe_count_kernel<KIND, OUTER, EJ_DESC_PACKED><<<grid, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount,
+                                                                                        pp.nwtiles, desc, ahead);
   else
-    probe_count_kernel<KIND, OUTER, false>
-        <<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles, nullptr,
-                                                            (uint64_t)h->num_sms * 5 * PR_WARPS);
+    probe_count_kernel<KIND, OUTER, EJ_DESC_WIDE><<<grid, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount,
+                                                                                      pp.nwtiles, desc, ahead);
   return ej_check_launch(h, "probe_count_kernel");
+}
+
+template <int KIND, bool OUTER>
+ej_status launch_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
+                       const void* desc, const unsigned long long* woff, ej_result* out, uint64_t cap) {
+  const uint64_t ahead = (uint64_t)h->num_sms * 4 * PR_WARPS;
+  const dim3 grid((unsigned)pp.ntiles);
+  if (desc_form(t) == EJ_DESC_PACKED)
+    probe_write_kernel<KIND, OUTER, EJ_DESC_PACKED><<<grid, PR_THREADS, 0, h->stream>>>(
+        P, desc, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
+  else
+    probe_write_kernel<KIND, OUTER, EJ_DESC_WIDE><<<grid, PR_THREADS, 0, h->stream>>>(
+        P, desc, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
+  return ej_check_launch(h, "probe_write_kernel");
 }
 
 }  // namespace
@@ -412,7 +442,7 @@ ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
                          bool outer, unsigned long long* d_count) {
   unsigned long long* wcount = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.count_off));
   unsigned long long* woff = reinterpret_cast<unsigned long long*>(ej_arena_at(h, pp.off_off));
-  uint2* desc = pp.with_desc ? reinterpret_cast<uint2*>(ej_arena_at(h, pp.desc_off)) : nullptr;
+  void* desc = pp.with_desc ? ej_arena_at(h, pp.desc_off) : nullptr;
   if (pp.ntiles) {
     if (t.kind == EJ_TABLE_HASH)
       EJ_TRY(outer ? launch_count<EJ_TABLE_HASH, true>(h, pp, P, t, wcount, desc)
@@ -429,15 +459,16 @@ ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
 }
 
 ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                         ej_result* out, uint64_t cap) {
+                         ej_result* out, uint64_t cap, bool outer) {
   if (!pp.ntiles) return EJ_OK;
   if (!pp.with_desc) return ej_fail(h, EJ_ERR_INTERNAL, "probe write planned without run descriptors");
-  const uint2* desc = reinterpret_cast<const uint2*>(ej_arena_at(h, pp.desc_off));
+  const void* desc = ej_arena_at(h, pp.desc_off);
   const unsigned long long* woff = reinterpret_cast<const unsigned long long*>(ej_arena_at(h, pp.off_off));
-  probe_write_kernel<<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(P, desc, pp.nP, t, woff, pp.nwtiles, out,
-                                                                        cap, h->d_status,
-                                                                        (uint64_t)h->num_sms * 4 * PR_WARPS);
-  return ej_check_launch(h, "probe_write_kernel");
+  if (t.kind == EJ_TABLE_HASH)
+    return outer ? launch_write<EJ_TABLE_HASH, true>(h, pp, P, t, desc, woff, out, cap)
+                 : launch_write<EJ_TABLE_HASH, false>(h, pp, P, t, desc, woff, out, cap);
+  return outer ? launch_write<EJ_TABLE_SORTED, true>(h, pp, P, t, desc, woff, out, cap)
+               : launch_write<EJ_TABLE_SORTED, false>(h, pp, P, t, desc, woff, out, cap);
 }
 
 // ---- partition bits for the probe side ------------------------------------
@@ -514,7 +545,7 @@ ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_v
   if (count_only || L.pp.with_desc) {  // the count pass, then (planned two-pass) rows in probe order
     EJ_TRY(ej_probe_count(h, L.pp, P, t, outer, d_count));
     ej_phase_mark(h, 3);
-    if (!count_only) EJ_TRY(ej_probe_write(h, L.pp, P, t, out, out_cap));
+    if (!count_only) EJ_TRY(ej_probe_write(h, L.pp, P, t, out, out_cap, outer));
   } else {
     ej_phase_mark(h, 3);  // one pass: recorded as the write phase
     EJ_TRY(ej_probe_fused(h, L.pp, P, t, outer, out, out_cap, d_count ? d_count : h->d_words + 3));

@@ -72,9 +72,9 @@ void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP, bool with
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                          bool outer, unsigned long long* d_count);
 // write pass from the run descriptors and offsets of ej_probe_count (same
-// plan, same inputs)
+// plan, same inputs, same outer flag)
 ej_status ej_probe_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
-                         ej_result* out, uint64_t cap);
+                         ej_result* out, uint64_t cap, bool outer = false);
 
 uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS);
 // two_pass: plan the run descriptors of ej_probe_count + ej_probe_write (for

@@ -231,13 +231,28 @@ __device__ __forceinline__ void ej_emit_warp(const EjProbeWarp& w, const int32_t
   if (fill) ej_flush_stage(stage, fill, a, out, cap);
 }
 
+// Run descriptors stored by the count pass for the write pass, in one of two
+// forms: EJ_DESC_WIDE, 8 bytes (lo, length); EJ_DESC_PACKED, 4 bytes
+// (lo << 5 | length) for tables of fewer than 2^27 rows, with the length
+// field EJ_PACKED_ESCAPE meaning "31 rows or more, or a NULL-extended row:
+// find the run again" (the write pass then repeats the find for its tile).
+enum { EJ_DESC_NONE = 0, EJ_DESC_WIDE = 1, EJ_DESC_PACKED = 2 };
+constexpr uint64_t EJ_PACKED_MAX_ROWS = 1ull << 27;
+constexpr uint32_t EJ_PACKED_ESCAPE = 31;
+
+__device__ __forceinline__ uint32_t ej_pack_run(uint32_t lo, uint32_t cnt) {
+  if (cnt == 0) return 0u;
+  if (cnt >= EJ_PACKED_ESCAPE || lo == NULL_RUN) return EJ_PACKED_ESCAPE;
+  return (lo << 5) | cnt;
+}
+
 // count pass of a warp tile; DESC: also stores each probe's run (lo, length)
-// in desc[probe] (OUTER: (NULL_RUN, 1) for a probe without matches).  Every
-// lane returns the warp tile's rows.
-template <int KIND, bool OUTER, bool DESC>
+// in desc[probe] (OUTER: (NULL_RUN, 1) for a probe without matches), wide or
+// packed.  Every lane returns the warp tile's rows.
+template <int KIND, bool OUTER, int DESC>
 __device__ __forceinline__ unsigned long long ej_probe_count_warp_desc(const ej_tuple* __restrict__ P, uint64_t base,
                                                                        uint64_t nP, const ej_table_view& t,
-                                                                       uint2* __restrict__ desc) {
+                                                                       void* __restrict__ desc) {
   const unsigned int lane = threadIdx.x & 31u;
   EjProbeWarp w;
   ej_probe_runs_warp<KIND, OUTER>(P, base, nP, t, w);
@@ -246,27 +261,41 @@ __device__ __forceinline__ unsigned long long ej_probe_count_warp_desc(const ej_
   for (int j = 0; j < PR_ITEMS; j++) {
     mine += w.cnt[j];
     const uint64_t idx = base + (uint64_t)j * 32 + lane;
-    if (DESC && idx < nP) __stcs(desc + idx, make_uint2(w.lo[j], w.cnt[j]));
+    if (DESC == EJ_DESC_WIDE && idx < nP) __stcs(static_cast<uint2*>(desc) + idx, make_uint2(w.lo[j], w.cnt[j]));
+    if (DESC == EJ_DESC_PACKED && idx < nP)
+      __stcs(static_cast<unsigned int*>(desc) + idx, ej_pack_run(w.lo[j], w.cnt[j]));
   }
   return ej_warp_sum<unsigned long long>(mine);
 }
 
-// write pass of a warp tile whose output starts at out[off]
-__device__ __forceinline__ void ej_probe_write_warp(const ej_tuple* __restrict__ P, const uint2* __restrict__ desc,
+// write pass of a warp tile whose output starts at out[off], from the
+// descriptors of the count pass (DESC: their form; a packed escape makes the
+// warp find its tile's runs again, KIND and OUTER as in the count pass)
+template <int KIND, bool OUTER, int DESC>
+__device__ __forceinline__ void ej_probe_write_warp(const ej_tuple* __restrict__ P, const void* __restrict__ desc,
                                                     uint64_t base, uint64_t nP, const ej_table_view& t,
                                                     unsigned long long off, ej_result* __restrict__ out,
                                                     uint64_t cap, int4* stage) {
   const unsigned int lane = threadIdx.x & 31u;
   EjProbeWarp w;
+  bool escape = false;
 #pragma unroll
   for (int j = 0; j < PR_ITEMS; j++) {
     const uint64_t idx = base + (uint64_t)j * 32 + lane;
     const bool ok = idx < nP;
     w.s[j] = ok ? __ldcs(reinterpret_cast<const int2*>(P) + idx) : make_int2(0, 0);
-    const uint2 d = ok ? __ldcs(desc + idx) : make_uint2(0u, 0u);
-    w.lo[j] = d.x;
-    w.cnt[j] = d.y;
+    if (DESC == EJ_DESC_PACKED) {
+      const uint32_t d = ok ? __ldcs(static_cast<const unsigned int*>(desc) + idx) : 0u;
+      w.lo[j] = d >> 5;
+      w.cnt[j] = d & 31u;
+      escape |= w.cnt[j] == EJ_PACKED_ESCAPE;
+    } else {
+      const uint2 d = ok ? __ldcs(static_cast<const uint2*>(desc) + idx) : make_uint2(0u, 0u);
+      w.lo[j] = d.x;
+      w.cnt[j] = d.y;
+    }
   }
+  if (DESC == EJ_DESC_PACKED && __any_sync(EJ_FULL_MASK, escape)) ej_probe_runs_warp<KIND, OUTER>(P, base, nP, t, w);
   int32_t kk[PR_ITEMS][PW_PREFETCH];
   ej_probe_prefetch(t, w, kk);
   ej_emit_warp(w, kk, t, off, out, cap, stage);
