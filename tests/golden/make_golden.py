@@ -1,7 +1,7 @@
 """Generate the golden fixtures that pin the oracle to the reference's own output.
 
-Run in a checkout that has the reference at $EJ_REFERENCE (default
-/root/reference); the GPU tests and the bench never run this script.
+Run with $EJ_REFERENCE naming the reference checkout; the GPU tests and the
+bench never run this script.
 
 1. join_ori known-answer fixture: the reference's binary tables
    joins/join_ori/R (1000 tuples) and S (100000 tuples) are stored compressed
@@ -43,7 +43,7 @@ from eating_one_gb300.workloads import distance_points, workload  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 from tests.golden import boundary_points  # noqa: E402
 
-REF = os.environ.get("EJ_REFERENCE", "/root/reference")
+REF = os.environ.get("EJ_REFERENCE", "")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref")
 
 # (program, workload, scale): R keys 1..|R|, S keys |R|+1..|R|+|S| as the
@@ -144,6 +144,8 @@ def distance_runs() -> list:
 
 
 def main() -> None:
+    if not os.path.isdir(os.path.join(REF, "joins")):
+        sys.exit("make_golden.py: set EJ_REFERENCE to the reference checkout (a directory holding joins/)")
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
     if "--distance-only" in sys.argv:
         with open(os.path.join(HERE, "reference_runs.json")) as f:
