@@ -5,16 +5,20 @@
 // For a stream of joins of uneven sizes (most of them small) that is launch-
 // and latency-bound.  Here a batch of joins is one fixed sequence of launches,
 // whatever the number of joins in it:
-//   build       four segmented LSD radix passes: tiles never cross a join and
+//   build       four segmented LSD radix passes over the joins that are not
+//               small: tiles never cross a join and
 //               the digit histograms are laid out join by join, so one scan
 //               places every join's rows in its own range, hash-sorted (the
 //               first pass reads every join's R where it lies)
 //   starts      every join's bucket starts in one launch (its own bucket bits;
 //               a batch's tables are small enough for L2, where the bucket
 //               scan is as fast as a key directory and one launch builds it)
-//   probe       one launch over every join's probe tiles: each warp finds its
-//               runs, reserves its rows with one atomic add on its join's
-//               count and writes them (the one-pass probe of single joins).
+//   probe       one resident launch over a work queue of tasks: whole small
+//               joins (R of at most 2048 rows: table built and probed in
+//               shared memory by one CTA, no radix pass) and the probe tiles
+//               of the others (each warp finds its runs, reserves its rows
+//               with one atomic add on its join's count and writes them, as
+//               the one-pass probe of single joins does).
 // Every join's rows are the rows it gives alone; their order within the join
 // is not specified (warps reserve their ranges in the order they arrive).
 #include "ej_device.cuh"
@@ -40,10 +44,14 @@ struct BatchJoin {
   const ej_tuple* R;
 };
 
-// global probe tile -> (join, tile of the join)
-struct BatchPTile {
+// a task of the batch's work queue: one probe tile of a join (local = the
+// tile), or a whole small join (local = BX_SMALL_TASK)
+struct BatchTask {
   uint32_t join, local;
 };
+constexpr uint32_t BX_SMALL_TASK = 0xFFFFFFFFu;
+// joins of at most this many R rows are built and probed in shared memory
+constexpr uint32_t BX_SMALL_R = 2048;
 
 // bucket bounds of every join: the block of one R tile fills the gaps
 // between the buckets of consecutive rows of its join; the join's last row
@@ -63,16 +71,13 @@ __global__ void batch_bucket_start_kernel(const ej_rx_tile* __restrict__ tiles, 
     ej_bucket_bounds_warp(t.rval, t.nR, r0, t.hb, bucket, EjHashBucketOf{t.hb});
 }
 
-// one pass over every join's probe tiles (block = one 1024-probe tile of one
-// join): each warp reserves its rows on its join's cursor (d_count, zeroed
-// before the launch), so the cursor ends at the join's count
-__global__ void __launch_bounds__(PR_THREADS)
-batch_fused_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __restrict__ ptiles, ej_dev_status* st) {
-  __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
-  const BatchPTile pt = ptiles[blockIdx.x];
-  const BatchJoin& j = joins[pt.join];
+// one probe tile of a join whose table the segmented passes built: each warp
+// reserves its rows on its join's cursor (d_count, zeroed before the launch),
+// so the cursor ends at the join's count
+__device__ __forceinline__ void batch_probe_tile(const BatchJoin& j, uint32_t local, int4 (*stage)[PW_STAGE_ROWS],
+                                                 ej_dev_status* st) {
   const unsigned int warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint64_t w = (uint64_t)pt.local * PR_WARPS + warp;
+  const uint64_t w = (uint64_t)local * PR_WARPS + warp;
   if (w >= j.nwtiles) return;
   EjProbeWarp pw;
   ej_probe_runs_warp<EJ_TABLE_HASH, false>(j.S, w * PR_WTILE, j.nS, j.view, pw);
@@ -93,6 +98,85 @@ batch_fused_kernel(const BatchJoin* __restrict__ joins, const BatchPTile* __rest
   ej_emit_warp(pw, kk, j.view, off, j.out, j.cap, stage[warp]);
 }
 
+// A join small enough for shared memory (nR <= BX_SMALL_R), whole, by one
+// CTA: R into a chained hash table in shared memory (bucket heads and row
+// links), then S probed 32 rows per warp and round: every lane walks its
+// row's chain twice, first counting, then - after one atomic add on the
+// join's cursor has reserved the warp's rows - writing them.  No radix pass,
+// no table in global memory.
+__device__ __forceinline__ void batch_small_join(const BatchJoin& j, int4* smem, ej_dev_status* st) {
+  int32_t* rk = reinterpret_cast<int32_t*>(smem);
+  int32_t* rv = rk + BX_SMALL_R;
+  int32_t* nxt = rv + BX_SMALL_R;
+  int32_t* head = nxt + BX_SMALL_R;
+  const uint32_t nR = (uint32_t)j.view.nR;
+  uint32_t nb = 1;
+  while (nb < nR) nb <<= 1;
+  for (uint32_t b = threadIdx.x; b < nb; b += PR_THREADS) head[b] = -1;
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < nR; i += PR_THREADS) {
+    const int2 r = reinterpret_cast<const int2*>(j.R)[i];
+    rk[i] = r.x;
+    rv[i] = r.y;
+    nxt[i] = atomicExch(&head[ej_hash32((uint32_t)r.y) & (nb - 1)], (int)i);
+  }
+  __syncthreads();
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint64_t base = (uint64_t)(threadIdx.x >> 5) * 32; base < j.nS; base += PR_THREADS) {
+    const uint64_t si = base + lane;
+    int2 s = make_int2(0, 0);
+    uint32_t c = 0;
+    int first = -1;
+    if (si < j.nS) {
+      s = __ldcs(reinterpret_cast<const int2*>(j.S) + si);
+      first = head[ej_hash32((uint32_t)s.y) & (nb - 1)];
+      for (int i = first; i >= 0; i = nxt[i]) c += rv[i] == s.y ? 1u : 0u;
+    }
+    const uint32_t incl = ej_warp_inclusive_sum<uint32_t>(c);
+    const uint32_t total = __shfl_sync(EJ_FULL_MASK, incl, 31);
+    if (total == 0) continue;
+    unsigned long long off = 0;
+    if (lane == 0) {
+      off = atomicAdd(j.d_count, (unsigned long long)total);
+      if (off + total > j.cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+    }
+    off = __shfl_sync(EJ_FULL_MASK, off, 0) + (incl - c);
+    for (int i = first; c && i >= 0; i = nxt[i]) {
+      if (rv[i] != s.y) continue;
+      if (off < j.cap) __stcs(reinterpret_cast<int4*>(j.out + off), make_int4(rk[i], s.y, s.x, s.y));
+      off++;
+    }
+  }
+}
+
+// The probe of a batch as one resident launch: every CTA takes tasks from a
+// work queue (an atomic counter over the task list) until it runs dry.  A
+// task is a whole small join (table built and probed in shared memory) or
+// one 1024-probe tile of a larger join (table from the segmented passes);
+// the small joins come first, so that no large task waits behind them at
+// the end.
+__global__ void __launch_bounds__(PR_THREADS)
+batch_queue_kernel(const BatchJoin* __restrict__ joins, const BatchTask* __restrict__ tasks, uint32_t ntasks,
+                   unsigned int* __restrict__ next_task, ej_dev_status* st) {
+  __shared__ int4 smem[PR_WARPS * PW_STAGE_ROWS];  // staging rows, or a small join's table
+  __shared__ uint32_t s_task;
+  static_assert(4 * BX_SMALL_R * sizeof(int32_t) <= sizeof(int4) * PR_WARPS * PW_STAGE_ROWS,
+                "a small join's table fits in the staging buffers");
+  for (;;) {
+    if (threadIdx.x == 0) s_task = atomicAdd(next_task, 1u);
+    __syncthreads();
+    const uint32_t k = s_task;
+    if (k >= ntasks) return;
+    const BatchTask task = tasks[k];
+    const BatchJoin& j = joins[task.join];
+    if (task.local == BX_SMALL_TASK)
+      batch_small_join(j, smem, st);
+    else
+      batch_probe_tile(j, task.local, reinterpret_cast<int4(*)[PW_STAGE_ROWS]>(smem), st);
+    __syncthreads();  // shared memory and s_task are reused by the next task
+  }
+}
+
 }  // namespace
 
 // Plan and launch; counts go to d_counts[i] (device).
@@ -100,7 +184,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   // host-side layout of the batch
   std::vector<BatchJoin> joins(n);
   std::vector<ej_rx_tile> rtiles;
-  std::vector<BatchPTile> ptiles;
+  std::vector<BatchTask> small_tasks, tile_tasks;
   std::vector<unsigned long long> sbase(n);
   uint64_t nr_total = 0, start_total = 0, cells = 0;
   for (uint32_t i = 0; i < n; i++) {
@@ -116,6 +200,12 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     b.view.kind = EJ_TABLE_HASH;
     b.view.nR = nR;
     b.view.hb = ej_table_bucket_bits(nR, ej_tuned_bucket_delta(h, nR));
+    b.nwtiles = (nS + PR_WTILE - 1) / PR_WTILE;
+    sbase[i] = start_total;
+    if (nR && nR <= BX_SMALL_R) {  // built and probed by one CTA in shared memory
+      if (nS) small_tasks.push_back({i, BX_SMALL_TASK});
+      continue;
+    }
     const uint32_t rt = (uint32_t)((nR + BX_RX_TILE - 1) / BX_RX_TILE);
     for (uint32_t t = 0; t < rt; t++) {
       ej_rx_tile d;
@@ -128,13 +218,14 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
       rtiles.push_back(d);
     }
     cells += (uint64_t)rt * 256;
-    sbase[i] = start_total;
     start_total += 1ull << b.view.hb;
-    b.nwtiles = (nS + PR_WTILE - 1) / PR_WTILE;
     const uint32_t nptiles = (uint32_t)((nS + PR_TILE - 1) / PR_TILE);
-    for (uint32_t t = 0; t < nptiles; t++) ptiles.push_back({i, t});
+    for (uint32_t t = 0; t < nptiles; t++) tile_tasks.push_back({i, t});
     nr_total += nR;
   }
+  // the work queue: small joins first, then every probe tile
+  std::vector<BatchTask> tasks(small_tasks);
+  tasks.insert(tasks.end(), tile_tasks.begin(), tile_tasks.end());
   if (cells > 0xFFFFFFFFull || nr_total >= 0xFFFFFFFFull)
     return ej_fail(h, EJ_ERR_TOO_LARGE, "batch of %llu R rows is too large", (unsigned long long)nr_total);
 
@@ -143,7 +234,8 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   const size_t joins_off = p.add(n * sizeof(BatchJoin));
   const size_t rtiles_off = p.add(std::max<size_t>(rtiles.size(), 1) * sizeof(ej_rx_tile));
   const size_t rtiles0_off = p.add(std::max<size_t>(rtiles.size(), 1) * sizeof(ej_rx_tile));
-  const size_t ptiles_off = p.add(std::max<size_t>(ptiles.size(), 1) * sizeof(BatchPTile));
+  const size_t tasks_off = p.add(std::max<size_t>(tasks.size(), 1) * sizeof(BatchTask));
+  const size_t queue_off = p.add(sizeof(unsigned int));
   const size_t sbase_off = p.add(n * sizeof(unsigned long long));
   const size_t tmpa_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
   const size_t tmpb_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
@@ -171,14 +263,15 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   }
   // descriptors go up with the batch (stream-ordered copies)
   const size_t jb = n * sizeof(BatchJoin), rb = rtiles.size() * sizeof(ej_rx_tile),
-               pb = ptiles.size() * sizeof(BatchPTile), sb = n * sizeof(unsigned long long);
+               pb = tasks.size() * sizeof(BatchTask), sb = n * sizeof(unsigned long long);
   EJ_CUDA(h, cudaMemcpyAsync(A + joins_off, joins.data(), jb, cudaMemcpyHostToDevice, h->stream));
   if (rb) EJ_CUDA(h, cudaMemcpyAsync(A + rtiles_off, rtiles.data(), rb, cudaMemcpyHostToDevice, h->stream));
   // the first radix pass reads every join's R where it lies: the same tiles
   // with their source rows
   for (ej_rx_tile& d : rtiles) d.src = joins[d.pad].R + (d.start - joins[d.pad].r_row0);
   if (rb) EJ_CUDA(h, cudaMemcpyAsync(A + rtiles0_off, rtiles.data(), rb, cudaMemcpyHostToDevice, h->stream));
-  if (pb) EJ_CUDA(h, cudaMemcpyAsync(A + ptiles_off, ptiles.data(), pb, cudaMemcpyHostToDevice, h->stream));
+  if (pb) EJ_CUDA(h, cudaMemcpyAsync(A + tasks_off, tasks.data(), pb, cudaMemcpyHostToDevice, h->stream));
+  EJ_CUDA(h, cudaMemsetAsync(A + queue_off, 0, sizeof(unsigned int), h->stream));
   EJ_CUDA(h, cudaMemcpyAsync(A + sbase_off, sbase.data(), sb, cudaMemcpyHostToDevice, h->stream));
   EJ_CUDA(h, cudaMemsetAsync(d_counts, 0, n * sizeof(unsigned long long), h->stream));
   const BatchJoin* djoins = reinterpret_cast<const BatchJoin*>(A + joins_off);
@@ -207,10 +300,19 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   ej_phase_mark(h, 1);
   ej_phase_mark(h, 2);  // no partition pass: every table of a batch is probed in place
   ej_phase_mark(h, 3);  // one pass: recorded as the write phase
-  if (!ptiles.empty()) {
-    const BatchPTile* dpt = reinterpret_cast<const BatchPTile*>(A + ptiles_off);
-    batch_fused_kernel<<<(unsigned)ptiles.size(), PR_THREADS, 0, h->stream>>>(djoins, dpt, h->d_status);
-    EJ_TRY(ej_check_launch(h, "batch_fused_kernel"));
+  if (!tasks.empty()) {
+    // one resident wave: as many CTAs as fit on the GPU at once, or fewer
+    // when the queue is shorter
+    static int per_sm = 0;
+    if (!per_sm) {
+      EJ_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_queue_kernel, PR_THREADS, 0));
+      if (per_sm < 1) per_sm = 1;
+    }
+    const uint64_t grid = std::min<uint64_t>(tasks.size(), (uint64_t)h->num_sms * per_sm);
+    batch_queue_kernel<<<(unsigned)grid, PR_THREADS, 0, h->stream>>>(
+        djoins, reinterpret_cast<const BatchTask*>(A + tasks_off), (uint32_t)tasks.size(),
+        reinterpret_cast<unsigned int*>(A + queue_off), h->d_status);
+    EJ_TRY(ej_check_launch(h, "batch_queue_kernel"));
   }
   ej_phase_mark(h, 4);
   return EJ_OK;
