@@ -286,12 +286,26 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
         pool = RequestPool(eng, 256)
         descs = (native.JoinDesc * len(pool.desc))(*pool.desc)
         d_counts = torch.zeros(len(pool.desc), dtype=torch.int64, device="cuda")
+        one_count = torch.zeros(1, dtype=torch.int64, device="cuda")
+        stream = torch.cuda.current_stream()
+        eng.batch_hash_join_async(descs, len(pool.desc), d_counts)  # warm-up: the arena grows once
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
         for _ in range(repeat):
             eng.batch_hash_join_async(descs, len(pool.desc), d_counts)
+        e1.record(stream)
+        # the same joins one pipeline each, on the same stream
+        for R, S, o in zip(pool.R, pool.S, pool.out):
+            eng.hash_join_async(R, S, o, one_count)
+        e2.record(stream)
         torch.cuda.synchronize()
         got = d_counts.cpu().tolist()
         assert got == pool.expected
-        print(json.dumps({"profile_case": name, "joins": len(got), "rows": int(sum(got))}), flush=True)
+        tuples = sum(pool.tuples(i) for i in range(len(pool.desc)))
+        print(json.dumps({"profile_case": name, "joins": len(got), "rows": int(sum(got)), "tuples": tuples,
+                          "batch_ms": round(e0.elapsed_time(e1) / repeat, 4),
+                          "per_join_ms": round(e1.elapsed_time(e2), 4)}), flush=True)
         return
     if name == "c4_star":  # `repeat` 3-way star joins of C4's fact and dimension tables
         w = workload("c4_star", scale)

@@ -13,7 +13,7 @@
 //   starts      every join's bucket starts in one launch (its own bucket bits;
 //               a batch's tables are small enough for L2, where the bucket
 //               scan is as fast as a key directory and one launch builds it)
-//   probe       one resident launch over a work queue of tasks: whole small
+//   probe       one launch over a task list, a task per block: whole small
 //               joins (R of at most 2048 rows: table built and probed in
 //               shared memory by one CTA, no radix pass) and the probe tiles
 //               of the others (each warp finds its runs, reserves its rows
@@ -44,7 +44,7 @@ struct BatchJoin {
   const ej_tuple* R;
 };
 
-// a task of the batch's work queue: one probe tile of a join (local = the
+// a task of the batch's task list: one probe tile of a join (local = the
 // tile), or a whole small join (local = BX_SMALL_TASK)
 struct BatchTask {
   uint32_t join, local;
@@ -149,32 +149,24 @@ __device__ __forceinline__ void batch_small_join(const BatchJoin& j, int4* smem,
   }
 }
 
-// The probe of a batch as one resident launch: every CTA takes tasks from a
-// work queue (an atomic counter over the task list) until it runs dry.  A
-// task is a whole small join (table built and probed in shared memory) or
-// one 1024-probe tile of a larger join (table from the segmented passes);
-// the small joins come first, so that no large task waits behind them at
-// the end.
+// The probe of a batch as one launch over a task list, one task per block,
+// handed out in list order by the block scheduler: a whole small join (table
+// built and probed in shared memory) or one 1024-probe tile of a larger join
+// (table from the segmented passes).  The small joins come first, so that no
+// large task waits behind them at the end.  (A resident grid pulling tasks
+// from an atomic counter measured slower: its loop needs 80 registers a
+// thread, three blocks per SM instead of four.)
 __global__ void __launch_bounds__(PR_THREADS)
-batch_queue_kernel(const BatchJoin* __restrict__ joins, const BatchTask* __restrict__ tasks, uint32_t ntasks,
-                   unsigned int* __restrict__ next_task, ej_dev_status* st) {
+batch_task_kernel(const BatchJoin* __restrict__ joins, const BatchTask* __restrict__ tasks, ej_dev_status* st) {
   __shared__ int4 smem[PR_WARPS * PW_STAGE_ROWS];  // staging rows, or a small join's table
-  __shared__ uint32_t s_task;
   static_assert(4 * BX_SMALL_R * sizeof(int32_t) <= sizeof(int4) * PR_WARPS * PW_STAGE_ROWS,
                 "a small join's table fits in the staging buffers");
-  for (;;) {
-    if (threadIdx.x == 0) s_task = atomicAdd(next_task, 1u);
-    __syncthreads();
-    const uint32_t k = s_task;
-    if (k >= ntasks) return;
-    const BatchTask task = tasks[k];
-    const BatchJoin& j = joins[task.join];
-    if (task.local == BX_SMALL_TASK)
-      batch_small_join(j, smem, st);
-    else
-      batch_probe_tile(j, task.local, reinterpret_cast<int4(*)[PW_STAGE_ROWS]>(smem), st);
-    __syncthreads();  // shared memory and s_task are reused by the next task
-  }
+  const BatchTask task = tasks[blockIdx.x];
+  const BatchJoin& j = joins[task.join];
+  if (task.local == BX_SMALL_TASK)
+    batch_small_join(j, smem, st);
+  else
+    batch_probe_tile(j, task.local, reinterpret_cast<int4(*)[PW_STAGE_ROWS]>(smem), st);
 }
 
 }  // namespace
@@ -223,7 +215,7 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
     for (uint32_t t = 0; t < nptiles; t++) tile_tasks.push_back({i, t});
     nr_total += nR;
   }
-  // the work queue: small joins first, then every probe tile
+  // the task list: small joins first, then every probe tile
   std::vector<BatchTask> tasks(small_tasks);
   tasks.insert(tasks.end(), tile_tasks.begin(), tile_tasks.end());
   if (cells > 0xFFFFFFFFull || nr_total >= 0xFFFFFFFFull)
@@ -235,7 +227,6 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   const size_t rtiles_off = p.add(std::max<size_t>(rtiles.size(), 1) * sizeof(ej_rx_tile));
   const size_t rtiles0_off = p.add(std::max<size_t>(rtiles.size(), 1) * sizeof(ej_rx_tile));
   const size_t tasks_off = p.add(std::max<size_t>(tasks.size(), 1) * sizeof(BatchTask));
-  const size_t queue_off = p.add(sizeof(unsigned int));
   const size_t sbase_off = p.add(n * sizeof(unsigned long long));
   const size_t tmpa_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
   const size_t tmpb_off = p.add(std::max<uint64_t>(nr_total, 1) * sizeof(ej_tuple));
@@ -271,7 +262,6 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   for (ej_rx_tile& d : rtiles) d.src = joins[d.pad].R + (d.start - joins[d.pad].r_row0);
   if (rb) EJ_CUDA(h, cudaMemcpyAsync(A + rtiles0_off, rtiles.data(), rb, cudaMemcpyHostToDevice, h->stream));
   if (pb) EJ_CUDA(h, cudaMemcpyAsync(A + tasks_off, tasks.data(), pb, cudaMemcpyHostToDevice, h->stream));
-  EJ_CUDA(h, cudaMemsetAsync(A + queue_off, 0, sizeof(unsigned int), h->stream));
   EJ_CUDA(h, cudaMemcpyAsync(A + sbase_off, sbase.data(), sb, cudaMemcpyHostToDevice, h->stream));
   EJ_CUDA(h, cudaMemsetAsync(d_counts, 0, n * sizeof(unsigned long long), h->stream));
   const BatchJoin* djoins = reinterpret_cast<const BatchJoin*>(A + joins_off);
@@ -301,18 +291,9 @@ static ej_status batch_run(ej_handle* h, const ej_join_desc* jd, uint32_t n, uns
   ej_phase_mark(h, 2);  // no partition pass: every table of a batch is probed in place
   ej_phase_mark(h, 3);  // one pass: recorded as the write phase
   if (!tasks.empty()) {
-    // one resident wave: as many CTAs as fit on the GPU at once, or fewer
-    // when the queue is shorter
-    static int per_sm = 0;
-    if (!per_sm) {
-      EJ_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_queue_kernel, PR_THREADS, 0));
-      if (per_sm < 1) per_sm = 1;
-    }
-    const uint64_t grid = std::min<uint64_t>(tasks.size(), (uint64_t)h->num_sms * per_sm);
-    batch_queue_kernel<<<(unsigned)grid, PR_THREADS, 0, h->stream>>>(
-        djoins, reinterpret_cast<const BatchTask*>(A + tasks_off), (uint32_t)tasks.size(),
-        reinterpret_cast<unsigned int*>(A + queue_off), h->d_status);
-    EJ_TRY(ej_check_launch(h, "batch_queue_kernel"));
+    batch_task_kernel<<<(unsigned)tasks.size(), PR_THREADS, 0, h->stream>>>(
+        djoins, reinterpret_cast<const BatchTask*>(A + tasks_off), h->d_status);
+    EJ_TRY(ej_check_launch(h, "batch_task_kernel"));
   }
   ej_phase_mark(h, 4);
   return EJ_OK;
