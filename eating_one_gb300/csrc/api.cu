@@ -200,6 +200,19 @@ extern "C" ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value) {
       if (value < -1 || value > 10000000000ll) return ej_fail(h, EJ_ERR_INVALID, "wait limit must be -1..1e10 ns");
       h->wait_limit_ns = value < 0 ? EJ_DEFAULT_WAIT_LIMIT_NS : (unsigned long long)value;
       return EJ_OK;
+    case EJ_OPT_BUILD:
+      if (value < EJ_BUILD_PLANNER || value > EJ_BUILD_MSD) return ej_fail(h, EJ_ERR_INVALID, "build must be 0..2");
+      h->opt_build = (int)value;
+      return EJ_OK;
+    case EJ_OPT_TABLE:
+      if (value < EJ_TABLE_FORMAT_PLANNER || value > EJ_TABLE_FORMAT_DIRECTORY)
+        return ej_fail(h, EJ_ERR_INVALID, "table format must be 0..2");
+      h->opt_table = (int)value;
+      return EJ_OK;
+    case EJ_OPT_PROBE_WARPS:
+      if (value != 0 && value != 4 && value != 8) return ej_fail(h, EJ_ERR_INVALID, "probe warps must be 0, 4 or 8");
+      h->opt_probe_warps = (int)value;
+      return EJ_OK;
     case EJ_OPT_COUNT_REUSE:
       if (value != 0 && value != 1) return ej_fail(h, EJ_ERR_INVALID, "count reuse is 0 or 1");
       h->opt_count_reuse = value != 0;
@@ -214,7 +227,9 @@ extern "C" ej_status ej_set_tuning(ej_handle* h, const ej_tune_entry* entries, u
   std::vector<ej_tune_entry> t(entries, entries + n);
   for (const ej_tune_entry& e : t) {
     if (e.log2_rows > 32 || e.partition_bits < -1 || e.partition_bits > 8 || e.bucket_delta < -3 ||
-        e.bucket_delta > 3)
+        e.bucket_delta > 3 || e.build < EJ_BUILD_PLANNER || e.build > EJ_BUILD_MSD ||
+        e.table < EJ_TABLE_FORMAT_PLANNER || e.table > EJ_TABLE_FORMAT_DIRECTORY ||
+        (e.probe_warps != 0 && e.probe_warps != 4 && e.probe_warps != 8))
       return ej_fail(h, EJ_ERR_INVALID, "bad tuning entry (log2_rows %u)", e.log2_rows);
   }
   std::sort(t.begin(), t.end(),
@@ -241,6 +256,24 @@ int ej_tuned_partition_bits(const ej_handle* h, uint64_t nR) {
   if (h->opt_partition_bits >= 0) return h->opt_partition_bits;
   const ej_tune_entry* e = tuning_for(h, nR);
   return e ? e->partition_bits : -1;
+}
+
+int ej_tuned_build(const ej_handle* h, uint64_t nR) {
+  if (h->opt_build) return h->opt_build;
+  const ej_tune_entry* e = tuning_for(h, nR);
+  return e ? e->build : EJ_BUILD_PLANNER;
+}
+
+int ej_tuned_table_format(const ej_handle* h, uint64_t nR) {
+  if (h->opt_table) return h->opt_table;
+  const ej_tune_entry* e = tuning_for(h, nR);
+  return e ? e->table : EJ_TABLE_FORMAT_PLANNER;
+}
+
+int ej_tuned_probe_warps(const ej_handle* h, uint64_t nR) {
+  if (h->opt_probe_warps) return h->opt_probe_warps;
+  const ej_tune_entry* e = tuning_for(h, nR);
+  return e && e->probe_warps ? e->probe_warps : 8;
 }
 
 extern "C" ej_status ej_last_phase_ms(ej_handle* h, float ms[EJ_PHASES]) {

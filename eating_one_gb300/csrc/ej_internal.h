@@ -60,6 +60,9 @@ struct ej_handle {
   int opt_partition_bits = -1;
   int opt_bucket_delta = 0;
   bool opt_bucket_delta_set = false;
+  int opt_build = 0;        // EJ_BUILD_* (0: tuning table, then planner)
+  int opt_table = 0;        // EJ_TABLE_FORMAT_*
+  int opt_probe_warps = 0;  // 4 or 8 (0: tuning table, then 8)
   std::vector<ej_tune_entry> tuning;  // ascending log2_rows
   // host-buffer entry points: device staging owned separately from the arena
   void* stage = nullptr;
@@ -236,3 +239,8 @@ uint32_t ej_table_bucket_bits(uint64_t nR, int delta = 0);
 // build side of nR rows: explicit options first, then the tuning table
 int ej_tuned_bucket_delta(const ej_handle* h, uint64_t nR);
 int ej_tuned_partition_bits(const ej_handle* h, uint64_t nR);
+// the build's radix passes, the table format (0: planner) and the probe
+// kernels' warps per block that apply to a build side of nR rows
+int ej_tuned_build(const ej_handle* h, uint64_t nR);
+int ej_tuned_table_format(const ej_handle* h, uint64_t nR);
+int ej_tuned_probe_warps(const ej_handle* h, uint64_t nR);

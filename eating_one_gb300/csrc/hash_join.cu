@@ -178,25 +178,27 @@ __device__ __forceinline__ void ej_prefetch_tile(const void* base, uint64_t w, u
   if (lane < 8u && off < nP * 8) asm volatile("prefetch.global.L2 [%0];" ::"l"(static_cast<const char*>(base) + off));
 }
 
-template <int KIND, bool OUTER, int DESC>
-__global__ void __launch_bounds__(PR_THREADS, 5)  // 40 warps per SM hide the table loads
+// The probe kernels come in two block shapes, WARPS = 8 or 4 warps of one
+// 128-probe warp tile each (EJ_OPT_PROBE_WARPS and the tuning table choose).
+template <int KIND, bool OUTER, int DESC, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 40 / WARPS)  // 40 warps per SM hide the table loads
 probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, unsigned long long* __restrict__ wcount,
                    uint64_t nwtiles, void* __restrict__ desc, uint64_t ahead) {
-  const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + (threadIdx.x >> 5);
+  const uint64_t w = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
   if (w >= nwtiles) return;
   ej_prefetch_tile(P, w + ahead, nP, threadIdx.x & 31u);  // the tile a warp one resident wave later takes
   const unsigned long long total = ej_probe_count_warp_desc<KIND, OUTER, DESC>(P, w * PR_WTILE, nP, t, desc);
   if ((threadIdx.x & 31u) == 0) wcount[w] = total;
 }
 
-template <int KIND, bool OUTER, int DESC>
-__global__ void __launch_bounds__(PR_THREADS)
+template <int KIND, bool OUTER, int DESC, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
 probe_write_kernel(const ej_tuple* __restrict__ P, const void* __restrict__ desc, uint64_t nP, ej_table_view t,
                    const unsigned long long* __restrict__ woff, uint64_t nwtiles, ej_result* __restrict__ out,
                    uint64_t cap, ej_dev_status* st, uint64_t ahead) {
-  __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
+  __shared__ int4 stage[WARPS][PW_STAGE_ROWS];
   const unsigned int warp = threadIdx.x >> 5;
-  const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + warp;
+  const uint64_t w = (uint64_t)blockIdx.x * WARPS + warp;
   if (w >= nwtiles) return;
   if (w == 0 && threadIdx.x == 0 && woff[nwtiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
   ej_prefetch_tile(P, w + ahead, nP, threadIdx.x & 31u);  // the tile a warp one resident wave later takes
@@ -220,14 +222,14 @@ probe_write_kernel(const ej_tuple* __restrict__ P, const void* __restrict__ desc
 // order is not deterministic (the multiset is); rows at or past cap are
 // dropped, the cursor ends at the exact count.  KEYS: how the run keys are
 // loaded (ej_probe_prefetch), fixed per table by the host.
-template <int KIND, bool OUTER, int KEYS>
-__global__ void __launch_bounds__(PR_THREADS)
+template <int KIND, bool OUTER, int KEYS, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
 probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t, uint64_t nwtiles,
                    unsigned long long* __restrict__ cursor, ej_result* __restrict__ out, uint64_t cap,
                    ej_dev_status* st, uint64_t ahead) {
-  __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
+  __shared__ int4 stage[WARPS][PW_STAGE_ROWS];
   const unsigned int warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + warp;
+  const uint64_t w = (uint64_t)blockIdx.x * WARPS + warp;
   if (w >= nwtiles) return;
   ej_prefetch_tile(P, w + ahead, nP, lane);  // the tile a warp one resident wave later takes
   EjProbeWarp pw;
@@ -256,35 +258,51 @@ probe_fused_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
 // from the same table view
 static int desc_form(const ej_table_view& t) { return t.nR < EJ_PACKED_MAX_ROWS ? EJ_DESC_PACKED : EJ_DESC_WIDE; }
 
+template <int KIND, bool OUTER, int WARPS>
+ej_status launch_count_w(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
+                         unsigned long long* wcount, void* desc) {
+  const uint64_t ahead = (uint64_t)h->num_sms * 40;  // warp tiles of one resident wave
+  const dim3 grid((unsigned)pp.ntiles);
+  constexpr int TH = WARPS * 32;
+  if (!desc)
+    probe_count_kernel<KIND, OUTER, EJ_DESC_NONE, WARPS><<<grid, TH, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles,
+                                                                                     nullptr, ahead);
+  else if (desc_form(t) == EJ_DESC_PACKED)
+    probe_count_kernel<KIND, OUTER, EJ_DESC_PACKED, WARPS><<<grid, TH, 0, h->stream>>>(P, pp.nP, t, wcount,
+                                                                                       pp.nwtiles, desc, ahead);
+  else
+    probe_count_kernel<KIND, OUTER, EJ_DESC_WIDE, WARPS><<<grid, TH, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles,
+                                                                                     desc, ahead);
+  return ej_check_launch(h, "probe_count_kernel");
+}
+
 template <int KIND, bool OUTER>
 ej_status launch_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                        unsigned long long* wcount, void* desc) {
-  const uint64_t ahead = (uint64_t)h->num_sms * 5 * PR_WARPS;
+  return pp.warps == 4 ? launch_count_w<KIND, OUTER, 4>(h, pp, P, t, wcount, desc)
+                       : launch_count_w<KIND, OUTER, 8>(h, pp, P, t, wcount, desc);
+}
+
+template <int KIND, bool OUTER, int WARPS>
+ej_status launch_write_w(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
+                         const void* desc, const unsigned long long* woff, ej_result* out, uint64_t cap) {
+  const uint64_t ahead = (uint64_t)h->num_sms * 32;  // warp tiles of one resident wave
   const dim3 grid((unsigned)pp.ntiles);
-  if (!desc)
-    probe_count_kernel<KIND, OUTER, EJ_DESC_NONE><<<grid, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount,
-                                                                                      pp.nwtiles, nullptr, ahead);
-  else if (desc_form(t) == EJ_DESC_PACKED)
-    probe_count_kernel<KIND, OUTER, EJ_DESC_PACKED><<<grid, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount,
-                                                                                        pp.nwtiles, desc, ahead);
+  constexpr int TH = WARPS * 32;
+  if (desc_form(t) == EJ_DESC_PACKED)
+    probe_write_kernel<KIND, OUTER, EJ_DESC_PACKED, WARPS><<<grid, TH, 0, h->stream>>>(
+        P, desc, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
   else
-    probe_count_kernel<KIND, OUTER, EJ_DESC_WIDE><<<grid, PR_THREADS, 0, h->stream>>>(P, pp.nP, t, wcount,
-                                                                                      pp.nwtiles, desc, ahead);
-  return ej_check_launch(h, "probe_count_kernel");
+    probe_write_kernel<KIND, OUTER, EJ_DESC_WIDE, WARPS><<<grid, TH, 0, h->stream>>>(
+        P, desc, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
+  return ej_check_launch(h, "probe_write_kernel");
 }
 
 template <int KIND, bool OUTER>
 ej_status launch_write(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                        const void* desc, const unsigned long long* woff, ej_result* out, uint64_t cap) {
-  const uint64_t ahead = (uint64_t)h->num_sms * 4 * PR_WARPS;
-  const dim3 grid((unsigned)pp.ntiles);
-  if (desc_form(t) == EJ_DESC_PACKED)
-    probe_write_kernel<KIND, OUTER, EJ_DESC_PACKED><<<grid, PR_THREADS, 0, h->stream>>>(
-        P, desc, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
-  else
-    probe_write_kernel<KIND, OUTER, EJ_DESC_WIDE><<<grid, PR_THREADS, 0, h->stream>>>(
-        P, desc, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
-  return ej_check_launch(h, "probe_write_kernel");
+  return pp.warps == 4 ? launch_write_w<KIND, OUTER, 4>(h, pp, P, t, desc, woff, out, cap)
+                       : launch_write_w<KIND, OUTER, 8>(h, pp, P, t, desc, woff, out, cap);
 }
 
 }  // namespace
@@ -309,13 +327,25 @@ size_t ej_table_aux_bytes(const ej_table_plan_t& tp) {
 
 size_t ej_table_col_bytes(uint64_t nR) { return (size_t)(nR + EJ_TABLE_PAD) * sizeof(int32_t); }
 
-void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta,
-                   uint64_t n_probe) {
+ej_table_knobs ej_tuned_table_knobs(const ej_handle* h, uint64_t nR) {
+  ej_table_knobs k;
+  k.delta = ej_tuned_bucket_delta(h, nR);
+  k.build = ej_tuned_build(h, nR);
+  k.table = ej_tuned_table_format(h, nR);
+  return k;
+}
+
+void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind,
+                   const ej_table_knobs& k, uint64_t n_probe) {
   tp.kind = kind;
   tp.nR = nR;
-  tp.prefer_dir = n_probe > 16 * nR;
-  tp.use_dir = kind == EJ_TABLE_HASH && (nR >= EJ_DIR_MIN_ROWS || (tp.prefer_dir && nR >= EJ_DIR_PROBE_MIN_ROWS));
-  tp.hb = ej_table_bucket_bits(nR, delta);  // hash buckets, or value buckets of a sorted table
+  // a directory chosen by the tuning is kept whatever the runs' length
+  tp.prefer_dir = n_probe > 16 * nR || k.table == EJ_TABLE_FORMAT_DIRECTORY;
+  tp.use_dir = kind == EJ_TABLE_HASH &&
+               (k.table == EJ_TABLE_FORMAT_DIRECTORY ||
+                (k.table == EJ_TABLE_FORMAT_PLANNER &&
+                 (nR >= EJ_DIR_MIN_ROWS || (tp.prefer_dir && nR >= EJ_DIR_PROBE_MIN_ROWS))));
+  tp.hb = ej_table_bucket_bits(nR, k.delta);  // hash buckets, or value buckets of a sorted table
   tp.passes = 4;  // all 32 key bits: equal keys end up adjacent
   if (!own_storage) {
     tp.rkey_off = p.add(ej_table_col_bytes(nR));
@@ -325,7 +355,8 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
   const size_t tuples = (size_t)(nR ? nR : 1) * sizeof(ej_tuple);
   tp.tmp_a_off = p.add(tuples);
   tp.tmp_b_off = p.add(tuples);
-  tp.msd = kind == EJ_TABLE_HASH && nR >= EJ_MSD_MIN_ROWS;
+  tp.msd = kind == EJ_TABLE_HASH &&
+           (k.build == EJ_BUILD_MSD || (k.build == EJ_BUILD_PLANNER && nR >= EJ_MSD_MIN_ROWS));
   if (tp.msd)
     ej_msd_plan_add(p, tp.mplan, nR);
   else
@@ -425,12 +456,11 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
 
 // ---- probe --------------------------------------------------------------
 
-uint64_t ej_probe_tiles(uint64_t nP) { return (nP + PR_TILE - 1) / PR_TILE; }
-
-void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP, bool with_desc) {
+void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP, bool with_desc, uint32_t warps) {
   pp.nP = nP;
-  pp.ntiles = ej_probe_tiles(nP);
+  pp.warps = warps == 4 ? 4u : 8u;
   pp.nwtiles = (nP + PR_WTILE - 1) / PR_WTILE;
+  pp.ntiles = (pp.nwtiles + pp.warps - 1) / pp.warps;
   pp.count_off = p.add((pp.nwtiles + 1) * sizeof(unsigned long long));
   pp.off_off = p.add((pp.nwtiles + 1) * sizeof(unsigned long long));
   pp.scan_off = p.add(ej_scan_scratch_bytes(pp.nwtiles));
@@ -493,26 +523,34 @@ uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS) {
 // ---- probe drivers -------------------------------------------------------
 
 void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only,
-                         bool two_pass) {
+                         bool two_pass, uint32_t warps) {
   L.pb = pb;
   if (pb) {
     L.spart_off = p.add((size_t)nS * sizeof(ej_tuple));
     ej_radix_plan_add(p, L.splan, nS);
   }
   (void)count_only;
-  ej_probe_plan(p, L.pp, nS, two_pass);
+  ej_probe_plan(p, L.pp, nS, two_pass, warps);
+}
+
+template <int KIND, bool OUTER, int WARPS>
+static ej_status launch_fused_w(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
+                                unsigned long long* cursor, ej_result* out, uint64_t cap) {
+  const uint64_t ahead = (uint64_t)h->num_sms * 32;  // warp tiles of one resident wave
+  if (t.short_runs)
+    probe_fused_kernel<KIND, OUTER, EJ_KEYS_CHUNKS, WARPS><<<(unsigned)pp.ntiles, WARPS * 32, 0, h->stream>>>(
+        P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, ahead);
+  else
+    probe_fused_kernel<KIND, OUTER, EJ_KEYS_WINDOW, WARPS><<<(unsigned)pp.ntiles, WARPS * 32, 0, h->stream>>>(
+        P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, ahead);
+  return ej_check_launch(h, "probe_fused_kernel");
 }
 
 template <int KIND, bool OUTER>
 static ej_status launch_fused(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
                               unsigned long long* cursor, ej_result* out, uint64_t cap) {
-  if (t.short_runs)
-    probe_fused_kernel<KIND, OUTER, EJ_KEYS_CHUNKS><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(
-        P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 32);
-  else
-    probe_fused_kernel<KIND, OUTER, EJ_KEYS_WINDOW><<<(unsigned)pp.ntiles, PR_THREADS, 0, h->stream>>>(
-        P, pp.nP, t, pp.nwtiles, cursor, out, cap, h->d_status, (uint64_t)h->num_sms * 32);
-  return ej_check_launch(h, "probe_fused_kernel");
+  return pp.warps == 4 ? launch_fused_w<KIND, OUTER, 4>(h, pp, P, t, cursor, out, cap)
+                       : launch_fused_w<KIND, OUTER, 8>(h, pp, P, t, cursor, out, cap);
 }
 
 // [partition +] the fused pass; the count ends in *cursor (zeroed here)
@@ -583,11 +621,11 @@ ej_status ej_hash_join_run(ej_handle* h, const ej_tuple* R, uint64_t nR, const e
   const uint32_t pb = (mode == 1) ? 0u : ej_probe_partition_bits(h, nR, nS);
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR), nS);
+  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_table_knobs(h, nR), nS);
   ej_probe_layout L;
   // the build-side-only join keeps its rows in probe order (the batched joins
   // give the same rows in the same order); the others take the one-pass probe
-  ej_probe_layout_add(p, L, nS, pb, mode == 2, /*two_pass=*/mode == 1 || keep);
+  ej_probe_layout_add(p, L, nS, pb, mode == 2, /*two_pass=*/mode == 1 || keep, ej_tuned_probe_warps(h, nR));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t;

@@ -39,7 +39,8 @@ struct ej_table_plan_t {
 
 struct ej_probe_plan_t {
   uint64_t nP = 0;
-  uint64_t ntiles = 0;   // blocks of 1024 probes
+  uint32_t warps = 8;    // warps (128-probe warp tiles) per block
+  uint64_t ntiles = 0;   // blocks of 128 * warps probes
   uint64_t nwtiles = 0;  // warp tiles of 128 probes
   size_t count_off = 0, off_off = 0, scan_off = 0;
   bool with_desc = false;  // run descriptors for the write pass
@@ -59,14 +60,21 @@ size_t ej_table_col_bytes(uint64_t nR);
 // bytes of the bucket bounds or the key directory (hash), or the value
 // buckets and their header (sorted)
 size_t ej_table_aux_bytes(const ej_table_plan_t& tp);
+// the tuned choices of a table's build (bucket-bits delta, EJ_BUILD_*,
+// EJ_TABLE_FORMAT_*; 0 in the last two: the planner's)
+struct ej_table_knobs {
+  int delta = 0;
+  int build = EJ_BUILD_PLANNER;
+  int table = EJ_TABLE_FORMAT_PLANNER;
+};
+ej_table_knobs ej_tuned_table_knobs(const ej_handle* h, uint64_t nR);
 // n_probe: the probe rows the caller expects (0: unknown)
-void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind, int delta = 0,
-                   uint64_t n_probe = 0);
+void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_storage, int kind,
+                   const ej_table_knobs& k = ej_table_knobs(), uint64_t n_probe = 0);
 ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple* R, int32_t* rkey, int32_t* rval,
                          void* aux, ej_table_view* view);
 
-uint64_t ej_probe_tiles(uint64_t nP);
-void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP, bool with_desc);
+void ej_probe_plan(ej_plan_bytes& p, ej_probe_plan_t& pp, uint64_t nP, bool with_desc, uint32_t warps = 8);
 // count pass (storing run descriptors when planned with them) + scan of the
 // warp-tile totals; the total goes to *d_count (device) when d_count != nullptr
 ej_status ej_probe_count(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple* P, const ej_table_view& t,
@@ -80,7 +88,7 @@ uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS);
 // two_pass: plan the run descriptors of ej_probe_count + ej_probe_write (for
 // callers that read the count in between); ej_probe_exec needs none
 void ej_probe_layout_add(ej_plan_bytes& p, ej_probe_layout& L, uint64_t nS, uint32_t pb, bool count_only,
-                         bool two_pass = false);
+                         bool two_pass = false, uint32_t warps = 8);
 ej_status ej_probe_exec(ej_handle* h, const ej_probe_layout& L, const ej_table_view& t, const ej_tuple* S,
                         bool outer, bool count_only, ej_result* out, uint64_t out_cap,
                         unsigned long long* d_count);

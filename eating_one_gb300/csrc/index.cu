@@ -84,7 +84,7 @@ static ej_status index_build(ej_handle* h, int kind, const ej_tuple* R, uint64_t
   *out = nullptr;
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/true, kind, ej_tuned_bucket_delta(h, nR));
+  ej_table_plan(p, tp, nR, /*own_storage=*/true, kind, ej_tuned_table_knobs(h, nR));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_index* ix = new ej_index();
   ix->kind = kind;
@@ -153,7 +153,7 @@ static ej_status index_probe(ej_handle* h, const ej_index* ix, const ej_tuple* S
   const uint32_t pb = ix->kind == EJ_TABLE_HASH ? ej_probe_partition_bits(h, ix->nR, nS) : 0u;
   ej_plan_bytes p;
   ej_probe_layout L;
-  ej_probe_layout_add(p, L, nS, pb, count_only);
+  ej_probe_layout_add(p, L, nS, pb, count_only, false, ej_tuned_probe_warps(h, ix->nR));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_phase_mark(h, 1);
@@ -211,9 +211,9 @@ extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_
   const uint32_t pb = ej_probe_partition_bits(h, nR, nS);
   ej_plan_bytes p;
   ej_table_plan_t tp;
-  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nR), nS);
+  ej_table_plan(p, tp, nR, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_table_knobs(h, nR), nS);
   ej_probe_layout L;
-  ej_probe_layout_add(p, L, nS, pb, /*count_only=*/false);
+  ej_probe_layout_add(p, L, nS, pb, /*count_only=*/false, false, ej_tuned_probe_warps(h, nR));
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t;
@@ -316,8 +316,10 @@ extern "C" ej_status ej_star_join3(ej_handle* h, const ej_tuple* F1, const ej_tu
   EJ_TRY(ej_check_out(h, out, out_cap, out_count));
   ej_plan_bytes p;
   ej_table_plan_t tp1, tp2;
-  ej_table_plan(p, tp1, nD1, false, EJ_TABLE_HASH, 0, nF);
-  ej_table_plan(p, tp2, nD2, false, EJ_TABLE_HASH, 0, nF);
+  ej_table_knobs k1 = ej_tuned_table_knobs(h, nD1), k2 = ej_tuned_table_knobs(h, nD2);
+  k1.delta = k2.delta = 0;  // the star join's dimension tables keep the default load factor
+  ej_table_plan(p, tp1, nD1, false, EJ_TABLE_HASH, k1, nF);
+  ej_table_plan(p, tp2, nD2, false, EJ_TABLE_HASH, k2, nF);
   EJ_TRY(ej_arena_reserve(h, p.bytes));
   ej_phase_begin(h);
   ej_table_view t1, t2;

@@ -348,7 +348,7 @@ extern "C" ej_status ej_join_host_chunked(ej_handle* h, ej_algo algo, const ej_t
     if (algo == EJ_ALGO_HASH) {
       ej_plan_bytes p;
       ej_table_plan_t tp;
-      ej_table_plan(p, tp, nb, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_bucket_delta(h, nb), nS);
+      ej_table_plan(p, tp, nb, /*own_storage=*/false, EJ_TABLE_HASH, ej_tuned_table_knobs(h, nb), nS);
       j.probe_base = p.bytes;
       j.pb = ej_probe_partition_bits(h, nb, s_chunk);
       ej_probe_layout L;

@@ -55,7 +55,9 @@ class Index:
 class Engine:
     """One ej_handle bound to one CUDA device."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, tuned: bool = True):
+        """tuned: install the tuning table measured on GB300
+        (eating_one_gb300/tuning_gb300.json, autotune.py) when it exists."""
         self.lib = native.load()
         self.device = torch.device("cuda", device)
         h = C.c_void_p()
@@ -63,6 +65,9 @@ class Engine:
         if st != native.EJ_OK:
             raise JoinError(st, "ej_create(%d) failed" % device)
         self.h = h
+        if tuned:
+            from . import autotune
+            autotune.load_default(self)
 
     # ---- plumbing -------------------------------------------------------------
     def close(self) -> None:
@@ -94,7 +99,8 @@ class Engine:
         self.lib.ej_set_stream(self.h, torch.cuda.current_stream(self.device).cuda_stream)
 
     def set_option(self, name: str, value: int) -> None:
-        opt = {"partition_bits": 0, "bucket_bits_delta": 1, "wait_limit_ns": 2, "count_reuse": 3}[name]
+        opt = {"partition_bits": 0, "bucket_bits_delta": 1, "wait_limit_ns": 2, "count_reuse": 3, "build": 4,
+               "table": 5, "probe_warps": 6}[name]
         self._check(self.lib.ej_set_option(self.h, opt, value))
 
     def set_timing(self, enable: bool) -> None:

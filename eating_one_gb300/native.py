@@ -100,10 +100,13 @@ class TuneEntry(C.Structure):
     """Mirror of ej_tune_entry (include/ej.h)."""
 
     _fields_ = [("log2_rows", C.c_uint32), ("partition_bits", C.c_int32), ("bucket_delta", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("build", C.c_int32), ("table", C.c_int32), ("probe_warps", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 EJ_SERVE_BATCHED, EJ_SERVE_PER_JOIN = 0, 1
+EJ_BUILD_PLANNER, EJ_BUILD_LSD, EJ_BUILD_MSD = 0, 1, 2
+EJ_TABLE_FORMAT_PLANNER, EJ_TABLE_FORMAT_BUCKETS, EJ_TABLE_FORMAT_DIRECTORY = 0, 1, 2
 EJ_TABLE_FILE_COUNTED, EJ_TABLE_FILE_RAW = 0, 1
 
 _vp, _u64, _pu64, _i32 = C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_int

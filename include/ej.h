@@ -132,23 +132,54 @@ typedef enum ej_option {
                                       results are then not valid); the handle stays usable.
                                       0 gives up at the first poll that finds a wait unmet, which
                                       lets tests drive the timeout path without a hung kernel */
-  EJ_OPT_COUNT_REUSE = 3           /* 1 (default): ej_hash_join_count keeps its table, partitioned
+  EJ_OPT_COUNT_REUSE = 3,          /* 1 (default): ej_hash_join_count keeps its table, partitioned
                                       S and run descriptors for an ej_hash_join that follows on the
                                       same relations; 0: the count keeps nothing (and writes no
                                       run descriptors) */
+  EJ_OPT_BUILD = 4,                /* radix passes of a hash table's build: EJ_BUILD_* (0: planner) */
+  EJ_OPT_TABLE = 5,                /* how probes find a hash table's runs: EJ_TABLE_FORMAT_* (0: planner) */
+  EJ_OPT_PROBE_WARPS = 6           /* block shape of the probe kernels: 4 or 8 warps of 32
+                                      threads per block (0: planner, 8) */
 } ej_option;
+
+/* Values of EJ_OPT_BUILD and ej_tune_entry.build.  The planner takes MSD for
+ * hash tables of 2^20 rows and more, else LSD; sorted indexes always sort by
+ * LSD passes (their key is the value, whose top bits need not spread). */
+enum {
+  EJ_BUILD_PLANNER = 0,
+  EJ_BUILD_LSD = 1, /* four stable 8-bit passes from the least significant digit */
+  EJ_BUILD_MSD = 2  /* two unordered 8-bit passes from the most significant digit,
+                       then a shared-memory sort of every 16-bit bucket */
+};
+/* Values of EJ_OPT_TABLE and ej_tune_entry.table.  The planner gives tables
+ * of 2^22 rows and more a key directory when their runs average two rows or
+ * more (tables of 2^20 rows and more when probed by 16 rows per table row or
+ * more), the others bucket bounds. */
+enum {
+  EJ_TABLE_FORMAT_PLANNER = 0,
+  EJ_TABLE_FORMAT_BUCKETS = 1,  /* bucket bounds: one 8-byte load, then a scan of the bucket */
+  EJ_TABLE_FORMAT_DIRECTORY = 2 /* key directory: one entry per distinct key, found by linear probing */
+};
 ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value);
 
 /* A tuning table (written by the autotuner, eating_one_gb300/autotune.py):
  * for joins whose build side has at least 2^log2_rows rows (the entry with the
- * largest such log2_rows applies), the S partition bits (-1: planner) and the
- * bucket-bits delta.  Options set with ej_set_option take precedence.
- * n = 0 clears the table. */
+ * largest such log2_rows applies), the S partition bits (-1: planner), the
+ * bucket-bits delta (the table's load factor), the build's radix passes
+ * (EJ_BUILD_*), the table format (EJ_TABLE_FORMAT_*) and the probe block shape
+ * (warps per block); 0 in the last three leaves the choice to the planner.
+ * Options set with ej_set_option take precedence.  n = 0 clears the table.
+ * The reference's counterpart is its commented per-size #define sets
+ * (joins/hashJoin_gpu/main_street/tuple.h:19-36,
+ * joins/innerJoin_gpu/main_street/tuple.h:9-34). */
 typedef struct ej_tune_entry {
   uint32_t log2_rows;
   int32_t partition_bits;
   int32_t bucket_delta;
-  int32_t reserved;
+  int32_t build;        /* EJ_BUILD_* */
+  int32_t table;        /* EJ_TABLE_FORMAT_* */
+  int32_t probe_warps;  /* 0, 4 or 8 */
+  int32_t reserved[2];  /* 0 */
 } ej_tune_entry;
 ej_status ej_set_tuning(ej_handle* h, const ej_tune_entry* entries, uint32_t n);
 
