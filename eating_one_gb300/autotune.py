@@ -106,11 +106,19 @@ def tune_class(eng: Engine, log2_rows: int, reps: int = 3, seed: int = 77) -> di
     return dict(best, log2_rows=log2_rows, ms=round(best_ms, 4), planner_ms=round(planner_ms, 4), trials=trials)
 
 
-def autotune(eng: Engine, classes=(10, 12, 14, 16, 18, 20, 22, 24, 26), reps: int = 3) -> list[dict]:
+def autotune(eng: Engine, classes=(10, 12, 14, 16, 18, 20, 22), reps: int = 3) -> list[dict]:
     """Tune every class; the engine's tuning table is cleared first (so that
-    "planner" means the planner) and left empty."""
+    "planner" means the planner) and left empty.  The table ends with an
+    entry one class above the last that hands every larger build side back to
+    the planner: the classes' workload is the served stream's request shape,
+    and beyond its sizes (2^22 rows) the right table format depends on the
+    data (the planner keeps a key directory when the table's runs average two
+    rows or more), which no single workload stands for."""
     load(eng, [])
-    return [tune_class(eng, c, reps) for c in classes]
+    table = [tune_class(eng, c, reps) for c in classes]
+    if table:
+        table.append(dict(PLANNER, log2_rows=max(classes) + 1, ms=None, planner_ms=None, trials=[]))
+    return table
 
 
 def load(eng: Engine, table: list[dict]) -> None:
@@ -138,7 +146,7 @@ def load_default(eng: Engine) -> bool:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=None)
-    ap.add_argument("--classes", default="10,12,14,16,18,20,22,24,26")
+    ap.add_argument("--classes", default="10,12,14,16,18,20,22")
     ap.add_argument("--reps", type=int, default=3)
     args = ap.parse_args()
     eng = Engine(0, tuned=False)

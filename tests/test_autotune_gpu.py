@@ -45,8 +45,9 @@ def test_every_knob_gives_the_oracle_rows(engine, build, table, warps):
 
 def test_autotune_small_classes(engine):
     table = autotune.autotune(engine, classes=(10, 14), reps=1)
-    assert [e["log2_rows"] for e in table] == [10, 14]
-    for e in table:
+    assert [e["log2_rows"] for e in table] == [10, 14, 15]
+    assert all(table[-1][k] == v for k, v in autotune.PLANNER.items())  # larger tables: the planner
+    for e in table[:-1]:
         assert e["partition_bits"] in (-1,) + autotune.PARTITION_CANDIDATES
         assert e["bucket_delta"] in autotune.DELTA_CANDIDATES
         assert e["build"] in (0,) + autotune.BUILD_CANDIDATES
