@@ -377,17 +377,22 @@ def run_serve(n_requests: int, n_instances: int, lanes: int) -> None:
 
     build()
     eng = Engine(0)
-    pool = RequestPool(eng, n_instances)
+    # every result is checked by its checksum (computed by the server on the
+    # device) against the instance's result alone; lanes x 1024 requests can be
+    # in flight, so each instance gets enough output buffers that no two of
+    # them write to the same one
+    copies = max(1, (lanes * 1024 + n_instances - 1) // n_instances)
+    pool = RequestPool(eng, n_instances, copies=copies, checksums=True)
     modes = {"batched": BATCHED, "per_join": PER_JOIN}
     res = {m: {} for m in modes}
     for name, mode in modes.items():
-        srv = Server(mode, lanes=lanes)
+        srv = Server(mode, lanes=lanes, checksums=True)
         run_stream(srv, pool, min(200, n_requests), None, seed=7)  # warm-up: arenas grow once
         res[name]["saturation"] = run_stream(srv, pool, n_requests, None, seed=8)
         srv.close()
     base_rate = res["per_join"]["saturation"]["requests_per_s"]
     for name, mode in modes.items():
-        srv = Server(mode, lanes=lanes)
+        srv = Server(mode, lanes=lanes, checksums=True)
         run_stream(srv, pool, min(200, n_requests), None, seed=7)
         res[name]["poisson"] = [run_stream(srv, pool, n_requests, f * base_rate, seed=10 + i)
                                 for i, f in enumerate(SERVE_SWEEP)]
@@ -410,7 +415,9 @@ def run_serve(n_requests: int, n_instances: int, lanes: int) -> None:
             "throughput_at_equal_p99": at_slo, "results": res,
             "saturation_ratio": res["batched"]["saturation"]["tuples_per_s"] /
                                 res["per_join"]["saturation"]["tuples_per_s"],
-            "wrong_results": wrong}
+            "wrong_results": wrong,
+            "checked": "every result: count and the order-independent checksum of its rows (computed on the device "
+                       "by the server) against the same join run alone"}
     print(json.dumps(line), flush=True)
     del torch
 

@@ -531,7 +531,38 @@ __global__ void checksum_kernel(const int32_t* __restrict__ w, uint64_t nrows, u
   if (threadIdx.x == 0) atomicAdd(acc, total);
 }
 
+// the checksums of many joins' outputs: block (x, y) sums the rows of join x
+// at positions y * 256 + t, y * 256 + t + gridDim.y * 256, ...
+__global__ void __launch_bounds__(256) checksum_outputs_kernel(const ej_join_desc* __restrict__ d,
+                                                               const unsigned long long* __restrict__ counts,
+                                                               unsigned long long* __restrict__ sums) {
+  __shared__ unsigned long long warp_tmp[256 / 32 + 1];
+  const ej_join_desc j = d[blockIdx.x];
+  const uint64_t rows = min((uint64_t)counts[blockIdx.x], j.out_cap);
+  const int4* out = reinterpret_cast<const int4*>(j.out);
+  unsigned long long sum = 0;
+  for (uint64_t i = (uint64_t)blockIdx.y * 256 + threadIdx.x; i < rows; i += (uint64_t)gridDim.y * 256) {
+    const int4 r = out[i];
+    uint64_t hsh = 0x243F6A8885A308D3ull;
+    hsh = ej_splitmix64(hsh ^ (uint64_t)(uint32_t)r.x);
+    hsh = ej_splitmix64(hsh ^ (uint64_t)(uint32_t)r.y);
+    hsh = ej_splitmix64(hsh ^ (uint64_t)(uint32_t)r.z);
+    sum += ej_splitmix64(hsh ^ (uint64_t)(uint32_t)r.w);
+  }
+  unsigned long long total;
+  ej_block_exclusive_sum<256, unsigned long long>(sum, warp_tmp, &total);
+  if (threadIdx.x == 0 && total) atomicAdd(sums + blockIdx.x, total);
+}
+
 }  // namespace
+
+ej_status ej_checksum_outputs_async(ej_handle* h, const ej_join_desc* d_desc, const unsigned long long* d_counts,
+                                    uint32_t n, unsigned long long* d_sums) {
+  if (!n) return EJ_OK;
+  EJ_CUDA(h, cudaMemsetAsync(d_sums, 0, n * sizeof(unsigned long long), h->stream));
+  checksum_outputs_kernel<<<dim3(n, 32), 256, 0, h->stream>>>(d_desc, d_counts, d_sums);
+  return ej_check_launch(h, "checksum_outputs_kernel");
+}
 
 // Zipf CDF over ranks 1..n with exponent s, built on the host in double
 // precision (the oracle builds its table with the same loop).

@@ -122,6 +122,10 @@ inline cudaError_t ej_pool_alloc(T** p, size_t bytes, cudaMemPool_t pool, cudaSt
 }
 
 ej_status ej_fail(ej_handle* h, ej_status s, const char* fmt, ...);
+// on the handle's stream: d_sums[i] = ej_checksum of the first
+// min(d_counts[i], d_desc[i].out_cap) rows of d_desc[i].out, i < n (device arrays)
+ej_status ej_checksum_outputs_async(ej_handle* h, const ej_join_desc* d_desc, const unsigned long long* d_counts,
+                                    uint32_t n, unsigned long long* d_sums);
 // frees the chunked-join resources (stream_join.cu); safe on a handle without them
 void ej_stream_release(ej_handle* h);
 // block nested loop over R x S (bnlj.cu); rows go to out at positions taken

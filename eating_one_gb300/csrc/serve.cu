@@ -55,6 +55,11 @@ struct Lane {
   cudaStream_t stream = nullptr;
   unsigned long long* d_counts = nullptr;
   unsigned long long* h_counts = nullptr;
+  // EJ_SERVE_CHECKSUM: the batch's requests and their outputs' checksums
+  ej_join_desc* d_desc = nullptr;
+  ej_join_desc* h_desc = nullptr;
+  unsigned long long* d_sums = nullptr;
+  unsigned long long* h_sums = nullptr;
   uint32_t cap = 0;
   bool busy = false;
   ej_status launch_status = EJ_OK;
@@ -85,6 +90,7 @@ void CUDART_CB lane_done(void* arg) {
       c.arrival_ns = r.arrival_ns;
       c.launch_ns = L->launch_ns;
       c.done_ns = now;
+      c.checksum = (S->cfg.flags & EJ_SERVE_CHECKSUM) ? L->h_sums[i] : 0;
       S->done.push_back(c);
     }
     S->completed += L->batch.size();
@@ -108,6 +114,18 @@ ej_status lane_launch(Lane* L, int mode) {
       const ej_join_desc& j = L->batch[i].join;
       st = ej_hash_join_async(h, j.R, j.nR, j.S, j.nS, j.out, j.out_cap, reinterpret_cast<uint64_t*>(L->d_counts + i));
     }
+  }
+  if (st == EJ_OK && (L->srv->cfg.flags & EJ_SERVE_CHECKSUM)) {
+    // the lane is busy until this batch completes, so h_desc is not rewritten
+    // before its copy runs
+    for (uint32_t i = 0; i < n; i++) L->h_desc[i] = L->batch[i].join;
+    if (cudaMemcpyAsync(L->d_desc, L->h_desc, n * sizeof(ej_join_desc), cudaMemcpyHostToDevice, L->stream) !=
+        cudaSuccess)
+      st = EJ_ERR_CUDA;
+    if (st == EJ_OK) st = ej_checksum_outputs_async(h, L->d_desc, L->d_counts, n, L->d_sums);
+    if (st == EJ_OK && cudaMemcpyAsync(L->h_sums, L->d_sums, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                       L->stream) != cudaSuccess)
+      st = EJ_ERR_CUDA;
   }
   if (st == EJ_OK && cudaMemcpyAsync(L->h_counts, L->d_counts, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                      L->stream) != cudaSuccess)
@@ -171,6 +189,10 @@ void server_free(Server* S) {
     if (L->stream) cudaStreamDestroy(L->stream);
     cudaFree(L->d_counts);
     cudaFreeHost(L->h_counts);
+    cudaFree(L->d_desc);
+    cudaFreeHost(L->h_desc);
+    cudaFree(L->d_sums);
+    cudaFreeHost(L->h_sums);
     delete L;
   }
   delete S;
@@ -206,7 +228,12 @@ extern "C" ej_status ej_server_create(const ej_server_config* cfg, ej_server** o
     }
     if (cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess ||
         ej_dev_alloc(&L->d_counts, per_lane * sizeof(unsigned long long)) != cudaSuccess ||
-        ej_host_alloc(&L->h_counts, per_lane * sizeof(unsigned long long)) != cudaSuccess) {
+        ej_host_alloc(&L->h_counts, per_lane * sizeof(unsigned long long)) != cudaSuccess ||
+        ((S->cfg.flags & EJ_SERVE_CHECKSUM) &&
+         (ej_dev_alloc(&L->d_desc, per_lane * sizeof(ej_join_desc)) != cudaSuccess ||
+          ej_host_alloc(&L->h_desc, per_lane * sizeof(ej_join_desc)) != cudaSuccess ||
+          ej_dev_alloc(&L->d_sums, per_lane * sizeof(unsigned long long)) != cudaSuccess ||
+          ej_host_alloc(&L->h_sums, per_lane * sizeof(unsigned long long)) != cudaSuccess))) {
       cudaGetLastError();
       server_free(S);
       return EJ_ERR_NOMEM;

@@ -82,14 +82,15 @@ class ServerConfig(C.Structure):
     """Mirror of ej_server_config (include/ej.h)."""
 
     _fields_ = [("device", C.c_int), ("mode", C.c_int), ("lanes", C.c_uint32), ("max_batch_joins", C.c_uint32),
-                ("lane_bytes", C.c_uint64), ("max_queued", C.c_uint32), ("reserved", C.c_uint32)]
+                ("lane_bytes", C.c_uint64), ("max_queued", C.c_uint32), ("flags", C.c_uint32)]
 
 
 class Completion(C.Structure):
     """Mirror of ej_completion (include/ej.h)."""
 
     _fields_ = [("tag", C.c_uint64), ("count", C.c_uint64), ("status", C.c_int32), ("batch_joins", C.c_uint32),
-                ("arrival_ns", C.c_uint64), ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64)]
+                ("arrival_ns", C.c_uint64), ("launch_ns", C.c_uint64), ("done_ns", C.c_uint64),
+                ("checksum", C.c_uint64)]
 
 
 class ChunkConfig(C.Structure):
@@ -105,6 +106,7 @@ class TuneEntry(C.Structure):
 
 
 EJ_SERVE_BATCHED, EJ_SERVE_PER_JOIN = 0, 1
+EJ_SERVE_CHECKSUM = 1
 EJ_BUILD_PLANNER, EJ_BUILD_LSD, EJ_BUILD_MSD = 0, 1, 2
 EJ_TABLE_FORMAT_PLANNER, EJ_TABLE_FORMAT_BUCKETS, EJ_TABLE_FORMAT_DIRECTORY = 0, 1, 2
 EJ_TABLE_FILE_COUNTED, EJ_TABLE_FILE_RAW = 0, 1

@@ -25,9 +25,13 @@ BATCHED, PER_JOIN = native.EJ_SERVE_BATCHED, native.EJ_SERVE_PER_JOIN
 
 class Server:
     def __init__(self, mode: int, device: int = 0, lanes: int = 2, max_batch_joins: int = 1024,
-                 lane_bytes: int = 16 << 30, max_queued: int = 0):
+                 lane_bytes: int = 16 << 30, max_queued: int = 0, checksums: bool = False):
+        """checksums: every completion carries the device-computed checksum of
+        its request's rows (EJ_SERVE_CHECKSUM)."""
         self.lib = native.load()
-        cfg = native.ServerConfig(device, mode, lanes, max_batch_joins, lane_bytes, max_queued, 0)
+        self.checksums = checksums
+        cfg = native.ServerConfig(device, mode, lanes, max_batch_joins, lane_bytes, max_queued,
+                                  native.EJ_SERVE_CHECKSUM if checksums else 0)
         h = C.c_void_p()
         st = self.lib.ej_server_create(C.byref(cfg), C.byref(h))
         if st != native.EJ_OK:
@@ -64,30 +68,45 @@ class Server:
 
 
 class RequestPool:
-    """Device-resident request instances of the C5 stream with their output buffers."""
+    """Device-resident request instances of the C5 stream with their output buffers.
+
+    copies > 1: every instance gets that many output buffers, each exactly as
+    large as its result (the stream's request i writes into buffer slot
+    i % (instances * copies)), so that requests of one instance in flight at
+    once write to different buffers - needed when every result is verified by
+    its checksum.  checksums: also record each instance's result checksum (its
+    rows joined alone, ej_single_hash_join)."""
 
     def __init__(self, engine: Engine, n_instances: int, seed: int = 0xE1A00005, lo_bits: float = 10.0,
-                 hi_bits: float = 22.0):
+                 hi_bits: float = 22.0, copies: int = 1, checksums: bool = False):
         rng = np.random.default_rng(seed)
+        self.ninst = n_instances
         self.R, self.S, self.out, self.desc, self.u = [], [], [], [], []
         for i in range(n_instances):
             nR = int(np.floor(2.0 ** (lo_bits + (hi_bits - lo_bits) * rng.random())))
             u = int(rng.choice([1, 2, 8]))
             d = nR * u
-            R = engine.generate(make_spec(EJ_GEN_PERM, nR, d, seed * 7 + 2 * i, seed * 7 + 2 * i + 1))
-            S = engine.generate(make_spec(EJ_GEN_UNIFORM, 4 * nR, d, seed * 11 + i))
-            out = torch.empty((4 * nR, 4), dtype=torch.int32, device=engine.device)  # every S row matches <= once
-            desc = native.JoinDesc(R.data_ptr(), nR, S.data_ptr(), 4 * nR, out.data_ptr(), 4 * nR)
-            self.R.append(R)
-            self.S.append(S)
-            self.out.append(out)
-            self.desc.append(desc)
+            self.R.append(engine.generate(make_spec(EJ_GEN_PERM, nR, d, seed * 7 + 2 * i, seed * 7 + 2 * i + 1)))
+            self.S.append(engine.generate(make_spec(EJ_GEN_UNIFORM, 4 * nR, d, seed * 11 + i)))
             self.u.append(u)
         torch.cuda.synchronize()
         self.expected = [engine.count("hash", R, S) for R, S in zip(self.R, self.S)]
+        self.expected_sum = [engine.checksum(engine.join("single_hash", R, S)) if checksums else None
+                             for R, S in zip(self.R, self.S)]
+        for c in range(copies):
+            for i in range(n_instances):
+                R, S = self.R[i], self.S[i]
+                # every S row matches at most once (unique R keys): 4|R| rows hold any result
+                cap = 4 * R.shape[0] if copies == 1 else max(self.expected[i], 1)
+                out = torch.empty((cap, 4), dtype=torch.int32, device=engine.device)
+                self.out.append(out)
+                self.desc.append(native.JoinDesc(R.data_ptr(), R.shape[0], S.data_ptr(), S.shape[0],
+                                                 out.data_ptr(), cap))
 
     def tuples(self, i: int) -> int:
-        return self.R[i].shape[0] + self.S[i].shape[0]
+        """Input tuples of request i (instance i % instances)."""
+        k = i % self.ninst
+        return self.R[k].shape[0] + self.S[k].shape[0]
 
 
 def run_stream(server: Server, pool: RequestPool, n_requests: int, rate_per_s: float | None, seed: int = 1) -> dict:
@@ -122,12 +141,15 @@ def run_stream(server: Server, pool: RequestPool, n_requests: int, rate_per_s: f
         server.submit(pool.desc[i % k], i, a)
     done.wait()
     th.join()
-    bad = [c.tag for c in comps if c.status != native.EJ_OK or c.count != pool.expected[c.tag % k]]
+    n = pool.ninst
+    bad = [c.tag for c in comps if c.status != native.EJ_OK or c.count != pool.expected[c.tag % n] or
+           (server.checksums and c.checksum != pool.expected_sum[c.tag % n])]
     lat = np.array([c.done_ns - c.arrival_ns for c in comps], dtype=np.float64) / 1e6
     first = min(c.arrival_ns for c in comps)
     last = max(c.done_ns for c in comps)
-    tuples = sum(pool.tuples(c.tag % k) for c in comps)
-    return {"requests": n_requests, "rate_per_s": rate_per_s, "p50_ms": float(np.percentile(lat, 50)),
+    tuples = sum(pool.tuples(c.tag) for c in comps)
+    return {"requests": n_requests, "rate_per_s": rate_per_s, "checked": "checksum" if server.checksums else "count",
+            "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "mean_batch": float(np.mean([c.batch_joins for c in comps])),
             "seconds": (last - first) / 1e9, "tuples_per_s": tuples / ((last - first) / 1e9),
             "requests_per_s": n_requests / ((last - first) / 1e9), "wrong": len(bad)}

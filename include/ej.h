@@ -330,8 +330,14 @@ typedef struct ej_server_config {
                                larger request still runs, alone */
   uint32_t max_queued;      /* requests waiting for a lane at once (0: no limit); a
                                submit past it is refused with EJ_ERR_BUSY */
-  uint32_t reserved;        /* 0 */
+  uint32_t flags;           /* EJ_SERVE_CHECKSUM, or 0 */
 } ej_server_config;
+
+/* ej_server_config.flags: after each batch, the lane computes on the device
+ * the order-independent checksum (ej_checksum's) of every request's rows and
+ * reports it in its completion, so that a client can verify each result
+ * without reading its rows back */
+#define EJ_SERVE_CHECKSUM 1u
 
 typedef struct ej_completion {
   uint64_t tag;          /* the submit tag */
@@ -341,6 +347,7 @@ typedef struct ej_completion {
   uint64_t arrival_ns;   /* ej_now_ns() clock: arrival, launch, completion */
   uint64_t launch_ns;
   uint64_t done_ns;
+  uint64_t checksum;     /* EJ_SERVE_CHECKSUM: ej_checksum of the request's rows (else 0) */
 } ej_completion;
 
 typedef struct ej_server ej_server;

@@ -54,3 +54,21 @@ def test_poisson_stream_counts(engine, pool):
     finally:
         srv.close()
     assert r["wrong"] == 0 and r["p99_ms"] >= r["p50_ms"] > 0
+
+
+@pytest.mark.parametrize("mode", [BATCHED, PER_JOIN])
+def test_served_results_checked_by_checksum(engine, mode):
+    """With EJ_SERVE_CHECKSUM every completion carries the checksum of its
+    request's rows, computed on the device; each must equal the checksum of
+    the same join run alone.  A planted wrong expectation (on the host) is
+    caught."""
+    pool = RequestPool(engine, 12, seed=5, lo_bits=10, hi_bits=15, copies=3, checksums=True)
+    srv = Server(mode, lanes=2, max_batch_joins=16, checksums=True)
+    try:
+        r = run_stream(srv, pool, 150, None, seed=3)
+        assert r["wrong"] == 0 and r["checked"] == "checksum"
+        pool.expected_sum[4] ^= 1
+        r = run_stream(srv, pool, 36, None, seed=4)
+        assert r["wrong"] == 3  # requests 4, 16 and 28
+    finally:
+        srv.close()
