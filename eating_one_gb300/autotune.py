@@ -5,8 +5,10 @@ join fastest, chosen by timing candidates on the device:
                   that many bits; the probe side's "passes" is 0 or 1)
   bucket_delta    the table's load factor: about 4 * 2^-delta R rows per bucket
   build           the table build's radix passes: EJ_BUILD_LSD (four stable
-                  8-bit passes) or EJ_BUILD_MSD (two unordered 8-bit passes
-                  and a shared-memory sort per 16-bit bucket)
+                  8-bit passes of three launches each), EJ_BUILD_MSD (two
+                  unordered 8-bit passes and a shared-memory sort per 16-bit
+                  bucket) or EJ_BUILD_ONESWEEP (four stable 8-bit passes of
+                  one launch each)
   table           how probes find runs: EJ_TABLE_FORMAT_BUCKETS (bucket
                   bounds) or EJ_TABLE_FORMAT_DIRECTORY (key directory)
   probe_warps     block shape of the probe kernels: 4 or 8 warps per block
@@ -42,7 +44,7 @@ TUNED_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning_g
 
 PARTITION_CANDIDATES = (0, 4, 6, 7, 8)
 DELTA_CANDIDATES = (-1, 0, 1)
-BUILD_CANDIDATES = (native.EJ_BUILD_LSD, native.EJ_BUILD_MSD)
+BUILD_CANDIDATES = (native.EJ_BUILD_LSD, native.EJ_BUILD_MSD, native.EJ_BUILD_ONESWEEP)
 TABLE_CANDIDATES = (native.EJ_TABLE_FORMAT_BUCKETS, native.EJ_TABLE_FORMAT_DIRECTORY)
 WARPS_CANDIDATES = (4, 8)
 KNOBS = ("partition_bits", "bucket_delta", "build", "table", "probe_warps")

@@ -201,7 +201,7 @@ extern "C" ej_status ej_set_option(ej_handle* h, ej_option opt, int64_t value) {
       h->wait_limit_ns = value < 0 ? EJ_DEFAULT_WAIT_LIMIT_NS : (unsigned long long)value;
       return EJ_OK;
     case EJ_OPT_BUILD:
-      if (value < EJ_BUILD_PLANNER || value > EJ_BUILD_MSD) return ej_fail(h, EJ_ERR_INVALID, "build must be 0..2");
+      if (value < EJ_BUILD_PLANNER || value > EJ_BUILD_ONESWEEP) return ej_fail(h, EJ_ERR_INVALID, "build must be 0..3");
       h->opt_build = (int)value;
       return EJ_OK;
     case EJ_OPT_TABLE:
@@ -227,7 +227,7 @@ extern "C" ej_status ej_set_tuning(ej_handle* h, const ej_tune_entry* entries, u
   std::vector<ej_tune_entry> t(entries, entries + n);
   for (const ej_tune_entry& e : t) {
     if (e.log2_rows > 32 || e.partition_bits < -1 || e.partition_bits > 8 || e.bucket_delta < -3 ||
-        e.bucket_delta > 3 || e.build < EJ_BUILD_PLANNER || e.build > EJ_BUILD_MSD ||
+        e.bucket_delta > 3 || e.build < EJ_BUILD_PLANNER || e.build > EJ_BUILD_ONESWEEP ||
         e.table < EJ_TABLE_FORMAT_PLANNER || e.table > EJ_TABLE_FORMAT_DIRECTORY ||
         (e.probe_warps != 0 && e.probe_warps != 4 && e.probe_warps != 8))
       return ej_fail(h, EJ_ERR_INVALID, "bad tuning entry (log2_rows %u)", e.log2_rows);

@@ -357,8 +357,14 @@ void ej_table_plan(ej_plan_bytes& p, ej_table_plan_t& tp, uint64_t nR, bool own_
   tp.tmp_b_off = p.add(tuples);
   tp.msd = kind == EJ_TABLE_HASH &&
            (k.build == EJ_BUILD_MSD || (k.build == EJ_BUILD_PLANNER && nR >= EJ_MSD_MIN_ROWS));
+  // onesweep only when chosen: its per-digit look-back measured slower than
+  // the three-launch LSD pass at every size (sort index of 2^24 rows: 0.68 vs
+  // 0.58 ms)
+  tp.onesweep = !tp.msd && k.build == EJ_BUILD_ONESWEEP;
   if (tp.msd)
     ej_msd_plan_add(p, tp.mplan, nR);
+  else if (tp.onesweep)
+    ej_onesweep_plan_add(p, tp.oplan, nR);
   else
     ej_radix_plan_add(p, tp.rplan, nR);
   if (tp.use_dir) {  // directory build scratch
@@ -386,7 +392,8 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
                       reinterpret_cast<ej_tuple*>(ej_arena_at(h, tp.tmp_b_off))};
   const ej_tuple* src = R;
   if (tp.msd) EJ_TRY(ej_msd_sort(h, tp.mplan, R, tmp[0], tmp[1], rkey, rval));
-  for (uint32_t p = 0; p < tp.passes && tp.nR && !tp.msd; p++) {
+  if (tp.onesweep) EJ_TRY(ej_onesweep_sort(h, tp.oplan, R, tmp[0], tmp[1], rkey, rval, digit_kind));
+  for (uint32_t p = 0; p < tp.passes && tp.nR && !tp.msd && !tp.onesweep; p++) {
     const uint32_t shift = 8u * p;
     if (p + 1 == tp.passes) {
       EJ_TRY(ej_radix_pass_soa(h, tp.rplan, src, rkey, rval, shift, 8u, digit_kind));

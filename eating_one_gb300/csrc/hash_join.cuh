@@ -7,6 +7,7 @@
 
 #include "ej_internal.h"
 #include "msd.cuh"
+#include "onesweep.cuh"
 
 // Hash tables of at least EJ_DIR_MIN_ROWS rows may carry a key directory (one
 // load per probe, seven build launches): the build keeps it when the table's
@@ -28,8 +29,10 @@ struct ej_table_plan_t {
   uint64_t nR = 0;
   uint32_t hb = 1;      // bucket bits (hash buckets, or value buckets of a sorted table)
   uint32_t passes = 4;  // LSD radix passes over the 32-bit key
-  bool msd = false;     // large hash tables: MSD passes + bucket sorts instead (msd.cuh)
+  bool msd = false;       // large hash tables: MSD passes + bucket sorts instead (msd.cuh)
   ej_msd_plan mplan;
+  bool onesweep = false;  // sorted indexes (and hash tables when chosen): one scatter launch per digit
+  ej_onesweep_plan oplan;
   // arena offsets; rkey/rval/aux are unused when the table has its own storage
   size_t rkey_off = 0, rval_off = 0, aux_off = 0, tmp_a_off = 0, tmp_b_off = 0;
   // key directory build scratch (hash tables)

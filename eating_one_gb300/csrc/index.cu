@@ -19,6 +19,7 @@
 #include "ej_entry.h"
 #include "hash_join.cuh"
 #include "probe.cuh"
+#include "probe_write.cuh"
 
 struct ej_index {
   int kind = EJ_TABLE_HASH;
@@ -202,6 +203,129 @@ extern "C" ej_status ej_sort_index_join(ej_handle* h, const ej_tuple* R, uint64_
 }
 
 // Left outer join on a transient hash table held in the arena.
+// ---- merge join of a sort index with S in value order ----------------------
+
+namespace {
+
+// Warp tile w: the 128 consecutive rows S[128 w ...] of an S in value order.
+// Their matches lie in the index rows between the first row at or above the
+// tile's first value and the first row above its last value; lanes 0 and 1
+// find those two bounds over the whole index (binary searches), then every
+// row's run is searched inside that window only - the merge of the two
+// sorted sequences cut into warp-sized pieces along S.  Rows are then written
+// as the one-pass probe writes them (one atomic reservation per warp).
+__global__ void __launch_bounds__(PR_THREADS)
+merge_probe_kernel(const ej_tuple* __restrict__ S, uint64_t nS, ej_table_view t, uint64_t nwtiles,
+                   unsigned long long* __restrict__ cursor, ej_result* __restrict__ out, uint64_t cap,
+                   ej_dev_status* st) {
+  __shared__ int4 stage[PR_WARPS][PW_STAGE_ROWS];
+  const unsigned int warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint64_t w = (uint64_t)blockIdx.x * PR_WARPS + warp;
+  if (w >= nwtiles) return;
+  const uint64_t base = w * PR_WTILE;
+  const uint64_t last = min(base + PR_WTILE, nS) - 1;
+  const int32_t* rv = t.rval;
+  const uint32_t nR = (uint32_t)t.nR;
+  // the window [wlo, whi) of the index: lane 0 the lower bound of the first
+  // value, lane 1 the upper bound of the last
+  uint32_t key1[1] = {0u}, lo1[1] = {0u}, hi1[1] = {nR};
+  if (lane < 2) key1[0] = ej_order_key<EJ_TABLE_SORTED>(reinterpret_cast<const int2*>(S)[lane ? last : base].y);
+  ej_search_rows<EJ_TABLE_SORTED, 1>(rv, lane < 2 && nR ? 1u : 0u, lane == 1, key1, lo1, hi1);
+  const uint32_t wlo = __shfl_sync(EJ_FULL_MASK, lo1[0], 0), whi = __shfl_sync(EJ_FULL_MASK, lo1[0], 1);
+  EjProbeWarp pw;
+  uint32_t key[PR_ITEMS], lo[PR_ITEMS], hi[PR_ITEMS], active = 0;
+#pragma unroll
+  for (int j = 0; j < PR_ITEMS; j++) {
+    const uint64_t idx = base + (uint64_t)j * 32 + lane;
+    const bool ok = idx < nS;
+    pw.s[j] = ok ? __ldcs(reinterpret_cast<const int2*>(S) + idx) : make_int2(0, 0);
+    key[j] = ej_order_key<EJ_TABLE_SORTED>(pw.s[j].y);
+    lo[j] = wlo;
+    hi[j] = whi;
+    if (ok && wlo < whi) active |= 1u << j;
+  }
+  // each run's first row, then (when it holds the value) its end
+  ej_search_rows<EJ_TABLE_SORTED, PR_ITEMS>(rv, active, false, key, lo, hi);
+  uint32_t found = 0, end[PR_ITEMS], top[PR_ITEMS];
+#pragma unroll
+  for (int j = 0; j < PR_ITEMS; j++) {
+    pw.lo[j] = lo[j];
+    pw.cnt[j] = 0;
+    end[j] = lo[j] + 1;
+    top[j] = whi;
+    if ((active >> j & 1u) && lo[j] < whi && __ldg(rv + lo[j]) == pw.s[j].y) {
+      pw.cnt[j] = 1;
+      if (end[j] < whi) found |= 1u << j;
+    }
+  }
+  ej_search_rows<EJ_TABLE_SORTED, PR_ITEMS>(rv, found, true, key, end, top);
+#pragma unroll
+  for (int j = 0; j < PR_ITEMS; j++)
+    if (found >> j & 1u) pw.cnt[j] = end[j] - pw.lo[j];
+  unsigned long long mine = 0;
+#pragma unroll
+  for (int j = 0; j < PR_ITEMS; j++) mine += pw.cnt[j];
+  const unsigned long long total = ej_warp_sum<unsigned long long>(mine);
+  if (total == 0) return;
+  int32_t kk[PR_ITEMS][PW_PREFETCH];
+  ej_probe_prefetch<EJ_KEYS_WINDOW>(t, pw, kk);
+  unsigned long long off = 0;
+  if (lane == 0) {
+    off = atomicAdd(cursor, total);
+    if (off + total > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
+  }
+  off = __shfl_sync(EJ_FULL_MASK, off, 0);
+  if (off >= cap) return;
+  ej_emit_warp(pw, kk, t, off, out, cap, stage[warp]);
+}
+
+}  // namespace
+
+extern "C" ej_status ej_index_merge_join(ej_handle* h, const ej_index* ix, const ej_tuple* S, uint64_t nS,
+                                         int s_sorted, ej_result* out, uint64_t out_cap, uint64_t* out_count) {
+  EJ_TRY(ej_begin(h));
+  if (!ix) return ej_fail(h, EJ_ERR_INVALID, "index is NULL");
+  if (ix->kind != EJ_TABLE_SORTED) return ej_fail(h, EJ_ERR_INVALID, "a merge join needs a sort index");
+  if (ix->device != h->device) return ej_fail(h, EJ_ERR_INVALID, "index lives on another device");
+  EJ_TRY(ej_check_rel(h, "S", S, nS));
+  EJ_TRY(ej_check_out(h, out, out_cap, out_count));
+  ej_plan_bytes p;
+  ej_radix_plan rp;
+  size_t a_off = 0, b_off = 0;
+  if (!s_sorted) {  // S in value order: four 8-bit LSD passes into a copy
+    a_off = p.add((size_t)(nS ? nS : 1) * sizeof(ej_tuple));
+    b_off = p.add((size_t)(nS ? nS : 1) * sizeof(ej_tuple));
+    ej_radix_plan_add(p, rp, nS);
+  }
+  EJ_TRY(ej_arena_reserve(h, p.bytes));
+  ej_phase_begin(h);
+  ej_phase_mark(h, 1);
+  const ej_tuple* P = S;
+  if (!s_sorted && nS) {
+    ej_tuple* a = reinterpret_cast<ej_tuple*>(ej_arena_at(h, a_off));
+    ej_tuple* b = reinterpret_cast<ej_tuple*>(ej_arena_at(h, b_off));
+    EJ_TRY(ej_partition_pass(h, rp, S, a, 0u, 8u, EJ_DIGIT_VALUE));  // the first pass needs no order
+    EJ_TRY(ej_radix_pass(h, rp, a, b, 8u, 8u, EJ_DIGIT_VALUE));
+    EJ_TRY(ej_radix_pass(h, rp, b, a, 16u, 8u, EJ_DIGIT_VALUE));
+    EJ_TRY(ej_radix_pass(h, rp, a, b, 24u, 8u, EJ_DIGIT_VALUE));
+    P = b;
+  }
+  ej_phase_mark(h, 2);
+  ej_phase_mark(h, 3);
+  EJ_CUDA(h, cudaMemsetAsync(h->d_words, 0, sizeof(unsigned long long), h->stream));
+  const uint64_t nwtiles = (nS + PR_WTILE - 1) / PR_WTILE;
+  if (nwtiles) {
+    merge_probe_kernel<<<(unsigned)((nwtiles + PR_WARPS - 1) / PR_WARPS), PR_THREADS, 0, h->stream>>>(
+        P, nS, ix->view, nwtiles, h->d_words, out, out_cap, h->d_status);
+    EJ_TRY(ej_check_launch(h, "merge_probe_kernel"));
+  }
+  ej_phase_mark(h, 4);
+  uint64_t count = 0;
+  EJ_TRY(ej_finish(h, &count));
+  *out_count = count;
+  return ej_capacity_result(h, count, out_cap);
+}
+
 extern "C" ej_status ej_left_outer_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
                                         uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count) {
   EJ_TRY(ej_begin(h));

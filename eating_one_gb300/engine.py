@@ -40,6 +40,13 @@ class Index:
         return self.engine._run_sized(lambda o, cap, cnt: self.engine.lib.ej_index_left_outer_join(
             self.engine.h, self.handle, _ptr(S), S.shape[0], o, cap, cnt), out, 4)
 
+    def merge_join(self, S: torch.Tensor, s_sorted: bool = False, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Merge join with S in value order (sort indexes; s_sorted False: the call sorts a copy of S)."""
+        if out is None:
+            out = torch.empty((self.count(S), 4), dtype=torch.int32, device=self.engine.device)
+        return self.engine._run_sized(lambda o, cap, cnt: self.engine.lib.ej_index_merge_join(
+            self.engine.h, self.handle, _ptr(S), S.shape[0], 1 if s_sorted else 0, o, cap, cnt), out, 4)
+
     def count(self, S: torch.Tensor) -> int:
         cnt = C.c_uint64(0)
         self.engine._check(self.engine.lib.ej_index_join_count(

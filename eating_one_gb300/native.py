@@ -107,7 +107,7 @@ class TuneEntry(C.Structure):
 
 EJ_SERVE_BATCHED, EJ_SERVE_PER_JOIN = 0, 1
 EJ_SERVE_CHECKSUM = 1
-EJ_BUILD_PLANNER, EJ_BUILD_LSD, EJ_BUILD_MSD = 0, 1, 2
+EJ_BUILD_PLANNER, EJ_BUILD_LSD, EJ_BUILD_MSD, EJ_BUILD_ONESWEEP = 0, 1, 2, 3
 EJ_TABLE_FORMAT_PLANNER, EJ_TABLE_FORMAT_BUCKETS, EJ_TABLE_FORMAT_DIRECTORY = 0, 1, 2
 EJ_TABLE_FILE_COUNTED, EJ_TABLE_FILE_RAW = 0, 1
 
@@ -142,6 +142,7 @@ _SIGS = {
     "ej_index_free": [_vp, _vp],
     "ej_index_join": [_vp, _vp, _vp, _u64, _vp, _u64, _pu64],
     "ej_index_join_count": [_vp, _vp, _vp, _u64, _pu64],
+    "ej_index_merge_join": [_vp, _vp, _vp, _u64, _i32, _vp, _u64, _pu64],
     "ej_hash_index_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_sort_index_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],
     "ej_left_outer_join": [_vp, _vp, _u64, _vp, _u64, _vp, _u64, _pu64],

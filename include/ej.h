@@ -143,13 +143,18 @@ typedef enum ej_option {
 } ej_option;
 
 /* Values of EJ_OPT_BUILD and ej_tune_entry.build.  The planner takes MSD for
- * hash tables of 2^20 rows and more, else LSD; sorted indexes always sort by
- * LSD passes (their key is the value, whose top bits need not spread). */
+ * hash tables of 2^20 rows and more, else LSD; sorted indexes sort by LSD
+ * passes (their key is the value, whose top bits need not spread, so MSD does
+ * not apply to them; EJ_BUILD_ONESWEEP applies to both kinds). */
 enum {
   EJ_BUILD_PLANNER = 0,
-  EJ_BUILD_LSD = 1, /* four stable 8-bit passes from the least significant digit */
-  EJ_BUILD_MSD = 2  /* two unordered 8-bit passes from the most significant digit,
-                       then a shared-memory sort of every 16-bit bucket */
+  EJ_BUILD_LSD = 1,      /* four stable 8-bit passes from the least significant digit,
+                            each a histogram, a scan and a scatter launch */
+  EJ_BUILD_MSD = 2,      /* two unordered 8-bit passes from the most significant digit,
+                            then a shared-memory sort of every 16-bit bucket (hash tables) */
+  EJ_BUILD_ONESWEEP = 3  /* four stable 8-bit LSD passes, one scatter launch each, after one
+                            histogram pass for all four digits (tiles learn their offsets
+                            by decoupled look-back) */
 };
 /* Values of EJ_OPT_TABLE and ej_tune_entry.table.  The planner gives tables
  * of 2^22 rows and more a key directory when their runs average two rows or
@@ -255,6 +260,17 @@ ej_status ej_index_join(ej_handle* h, const ej_index* idx, const ej_tuple* S, ui
                         ej_result* out, uint64_t out_cap, uint64_t* out_count);
 ej_status ej_index_join_count(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS,
                               uint64_t* out_count);
+/* Merge join of a sort index with S in value order: S's rows, 128 at a time,
+ * take the window of the index between the first row at or above their first
+ * value and the first row above their last, and find their runs inside it -
+ * the two sorted sequences merged piece by piece along S, instead of one
+ * search over the whole index per S row (sort_index/main_street/
+ * join_gpu.cu:10-113).  s_sorted != 0: S is already ordered by val (signed);
+ * 0: the call first sorts a copy of S in the handle's scratch (four LSD
+ * passes).  Rows come in no particular order; the index must be a sort
+ * index (EJ_ERR_INVALID otherwise). */
+ej_status ej_index_merge_join(ej_handle* h, const ej_index* idx, const ej_tuple* S, uint64_t nS, int s_sorted,
+                              ej_result* out, uint64_t out_cap, uint64_t* out_count);
 /* Build + probe in one call, timed like the reference (index build then join). */
 ej_status ej_hash_index_join(ej_handle* h, const ej_tuple* R, uint64_t nR, const ej_tuple* S,
                              uint64_t nS, ej_result* out, uint64_t out_cap, uint64_t* out_count);

@@ -20,7 +20,7 @@ def dev(a):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.int32)).cuda()
 
 
-@pytest.mark.parametrize("build", [native.EJ_BUILD_LSD, native.EJ_BUILD_MSD])
+@pytest.mark.parametrize("build", [native.EJ_BUILD_LSD, native.EJ_BUILD_MSD, native.EJ_BUILD_ONESWEEP])
 @pytest.mark.parametrize("table", [native.EJ_TABLE_FORMAT_BUCKETS, native.EJ_TABLE_FORMAT_DIRECTORY])
 @pytest.mark.parametrize("warps", [4, 8])
 def test_every_knob_gives_the_oracle_rows(engine, build, table, warps):
@@ -32,7 +32,8 @@ def test_every_knob_gives_the_oracle_rows(engine, build, table, warps):
     for name, v in (("build", build), ("table", table), ("probe_warps", warps), ("partition_bits", 5)):
         engine.set_option(name, v)
     try:
-        got = {a: engine.join(a, dev(R), dev(S)) for a in ("hash", "single_hash", "left_outer", "hash_index")}
+        got = {a: engine.join(a, dev(R), dev(S))
+               for a in ("hash", "single_hash", "left_outer", "hash_index", "sort_index")}
         out = torch.empty((len(O.hash_join(R, S)), 4), dtype=torch.int32, device="cuda")
         got["one_pass"] = engine.hash_join(dev(R), dev(S), out=out)  # no count before it
     finally:

@@ -297,6 +297,36 @@ def test_index_reuse_and_count(engine):
             ix.free()
 
 
+@pytest.mark.parametrize("case", [0, 1, 2, 4, 6, 7])
+def test_sort_index_merge_join(engine, case):
+    """The merge join of a sort index with S in value order gives the oracle's
+    rows, whether the call sorts S or the caller passes it sorted."""
+    nR, nS, (lo, hi) = CASES[case]
+    rng = np.random.default_rng(300 + case)
+    R, S = rel(rng, nR, lo, hi), rel(rng, nS, lo, hi, key_base=nR)
+    ref = O.sort_index_join(R, S)
+    ix = engine.build_index("sort", dev(R))
+    try:
+        same_multiset(ix.merge_join(dev(S)), ref)
+        order = np.argsort(S[:, 1], kind="stable")
+        same_multiset(ix.merge_join(dev(S[order]), s_sorted=True), ref)
+        if len(ref) > 2:  # capacity: the count, nothing written past out_cap
+            out = torch.full((len(ref) // 2 + 16, 4), -5, dtype=torch.int32, device="cuda")
+            with pytest.raises(JoinError) as ei:
+                ix.merge_join(dev(S), out=out[: len(ref) // 2])
+            assert ei.value.status == native.EJ_ERR_CAPACITY
+            assert torch.all(out[len(ref) // 2:] == -5)
+    finally:
+        ix.free()
+    hx = engine.build_index("hash", dev(R))
+    try:
+        with pytest.raises(JoinError) as ei:
+            hx.merge_join(dev(S))
+        assert ei.value.status == native.EJ_ERR_INVALID
+    finally:
+        hx.free()
+
+
 def test_star_join(engine):
     w = workload("c4_star", scale=8)
     t = {k: O.generate(v) for k, v in w.items()}
