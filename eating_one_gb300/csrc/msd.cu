@@ -150,14 +150,18 @@ __device__ __forceinline__ void ls_scan_digits(uint32_t* c, uint32_t* warp_tmp) 
 // The CTA sorts the rows [a, a + len) of `src` by hash bits 0..7 (all of them
 // share bits 8..31) into rkey/rval at the same positions: a counting sort
 // through global memory (order among equal hashes, which are equal keys,
-// unspecified).  Shared counters: sm.cnt2.
-__device__ void ls_digit_global(LsSmem& sm, const ej_tuple* __restrict__ src, uint64_t a, uint32_t len,
+// unspecified).  Shared counters: sm.cnt2.  `src` was written earlier in this
+// launch (by this CTA), so it is read through L2 (__ldcg), never through the
+// read-only cache, which another CTA on the SM may have filled with the same
+// lines before they were written; a stale line would make the two loops
+// below see different rows.
+__device__ void ls_digit_global(LsSmem& sm, const ej_tuple* src, uint64_t a, uint32_t len,
                                 int32_t* __restrict__ rkey, int32_t* __restrict__ rval) {
   sm.cnt2[threadIdx.x] = 0;
   __syncthreads();
   const uint2* s2 = reinterpret_cast<const uint2*>(src);
   for (uint32_t j = threadIdx.x; j < len; j += LS_THREADS)
-    atomicAdd(&sm.cnt2[ej_hash32(s2[a + j].y) & 255u], 1u);
+    atomicAdd(&sm.cnt2[ej_hash32(__ldcg(s2 + a + j).y) & 255u], 1u);
   __syncthreads();
   uint32_t c = sm.cnt2[threadIdx.x];
   uint32_t total;
@@ -165,10 +169,12 @@ __device__ void ls_digit_global(LsSmem& sm, const ej_tuple* __restrict__ src, ui
   sm.cnt2[threadIdx.x] = ex;
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < len; j += LS_THREADS) {
-    const uint2 x = s2[a + j];
+    const uint2 x = __ldcg(s2 + a + j);
     const uint32_t p = atomicAdd(&sm.cnt2[ej_hash32(x.y) & 255u], 1u);
-    rkey[a + p] = (int32_t)x.x;
-    rval[a + p] = (int32_t)x.y;
+    if (p < len) {  // always; a guard that keeps every store inside the range
+      rkey[a + p] = (int32_t)x.x;
+      rval[a + p] = (int32_t)x.y;
+    }
   }
   __syncthreads();
 }
@@ -198,7 +204,7 @@ __device__ void ls_bucket_global(LsSmem& sm, const ej_tuple* __restrict__ in, ej
   for (uint32_t j = threadIdx.x; j < m; j += LS_THREADS) {
     const uint2 x = s2[lo + j];
     const uint32_t p = atomicAdd(&cur[(ej_hash32(x.y) >> 8) & 255u], 1u);
-    t2[lo + p] = x;
+    if (p < m) t2[lo + p] = x;  // always; a guard that keeps every store inside the range
   }
   __syncthreads();  // the CTA's own global writes are visible to it past the barrier
   for (uint32_t s = 0; s < 256; s++) {
