@@ -683,10 +683,12 @@ def main() -> None:
               "probe_count_kernel", "probe_write_kernel"]
     # algorithmic bytes per launch of each phase: the build reads R once and
     # writes its two columns (16 B per row), the partition reads and writes S
-    # (16 B per tuple), the count reads the probe and writes its descriptor
-    # (16 B per probe), the write reads the probe and its descriptor and writes
-    # the rows (16 B per probe + 16 B per row)
-    phase_bytes = [16.0 * n_r, 16.0 * n_s, 16.0 * n_s, 16.0 * n_s + 16.0 * n_o]
+    # (16 B per tuple), the count reads the probe and writes its run
+    # descriptor, the write reads the probe and its descriptor and writes the
+    # rows (16 B per row); descriptors are 4 bytes for tables under 2^27 rows
+    # (C3's 2^26), else 8
+    desc = 4.0 if n_r < (1 << 27) else 8.0
+    phase_bytes = [16.0 * n_r, 16.0 * n_s, (8.0 + desc) * n_s, (8.0 + desc) * n_s + 16.0 * n_o]
     per_join = [p / nj for p in phases]
     dom = max(range(4), key=lambda i: per_join[i])
     achieved = phase_bytes[dom] / (per_join[dom] / 1000.0) / 1e9
@@ -764,7 +766,7 @@ def main() -> None:
                      "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                      "traffic_source": "not measured in this run: dram__bytes_read.sum + dram__bytes_write.sum "
                                        "of a 1/8-size ncu capture of the same kernel, scaled by 8 "
-                                       "(profiles/traffic_c3.json)",
+                                       "(profiles/traffic_c3.json, with the command that made it)",
                      "peak_source": peaks["source"],
                      "bytes_per_launch": int(phase_bytes[dom]), "ms_per_launch": round(per_join[dom], 4)},
         "join_roofline": {"alg_bytes_per_step": int(alg), "achieved": round(join_gbs, 1), "unit": "GB/s",
