@@ -331,6 +331,14 @@ def run_profile_case(name: str, scale: int, repeat: int) -> None:
         print(json.dumps({"profile_case": name, "scale": scale, "R": int(R.shape[0]), "S": int(S.shape[0]),
                           "rows": n_out}), flush=True)
         return
+    if name == "c3_build":  # `repeat` hash tables built on C3's R (the join's build phase alone)
+        w = workload("c3_s1.0", scale)
+        R = eng.generate(w["R"])
+        for _ in range(repeat):
+            eng.build_index("hash", R).free()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": name, "scale": scale, "R": int(R.shape[0])}), flush=True)
+        return
     if name in ("d2", "d3"):  # distance joins: dist_screen_kernel x2 + dist_kernel per call
         from eating_one_gb300.native import point_result_dtype
         from eating_one_gb300.workloads import distance_workload

@@ -6,7 +6,10 @@
 // {hash, run start} placed by linear probing from its home slot
 // hash >> (32 - bits), 2^bits >= 2 x keys: key k goes to
 //   pos_k = max(home_k, pos_{k-1} + 1) = k + max_{j <= k} (home_j - j),
-// so the entries stay in hash order.  Every slot holds the first key at or
+// so the entries stay in hash order.  Tables under 2^27 rows pack an entry
+// as {hash, start << 5 | run length} (31: 31 rows or more, the run then ends
+// at the next slot's start), so that one 8-byte load answers most probes;
+// larger tables keep {hash, start}.  Every slot holds the first key at or
 // after it: the slots between pos_{k-1} and pos_k hold copies of key k, the
 // slots past the last entry a sentinel {0xFFFFFFFF, nR}.  A probe walks
 // forward from its home slot past smaller hashes; it has found its key when
@@ -32,6 +35,8 @@ struct DirHeader {
   uint32_t hash0;  // hash of the first key
   unsigned long long nkeys;
   unsigned long long pos_first, pos_last;  // slots of the first and last entries
+  uint32_t lead;  // packed entries: the first key's {start << 5 | run length}
+  uint32_t pad;
 };
 constexpr size_t DIR_HEADER_BYTES = 256;
 
@@ -146,10 +151,12 @@ __device__ __forceinline__ long long dir_tile_max(const int32_t* __restrict__ rv
 }
 
 // the tile at row0 (first key rank k0, largest home_j - j of the keys before
-// it: kpre): every key's slots (pos_{k-1}, pos_k], holding {hash_k, start_k};
-// the first and last keys record their slots in the header
+// it: kpre): every key's slots (pos_{k-1}, pos_k], holding {hash_k, start_k}
+// or, packed, {hash_k, start_k << 5 | min(run length, 31)}; the first and
+// last keys record their slots in the header
 __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval, uint64_t n, uint64_t row0,
-                                               uint64_t k0, long long kpre, DirHeader* hdr, uint2* __restrict__ dir) {
+                                               uint64_t k0, long long kpre, DirHeader* hdr, uint2* __restrict__ dir,
+                                               bool packed) {
   __shared__ uint32_t tmp[DIR_THREADS / 32 + 1];
   __shared__ long long tmpl[DIR_THREADS / 32];
   const uint64_t i0 = row0 + threadIdx.x * DIR_ROWS;
@@ -170,16 +177,38 @@ __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval,
   long long all;
   long long run = max(kpre, dir_block_exclusive_max(m, tmpl, &all));  // max over keys before k
   long long prev = k ? (long long)k - 1 + run : -1;                   // pos_{k-1}
+  // a key's run ends at the thread's next key, else at the thread's last row
+  // plus `tail`: the rows after the thread's that continue its last key
+  // (counted up to a run of 31)
+  const uint32_t rows = i0 < n ? (uint32_t)min((uint64_t)DIR_ROWS, n - i0) : 0u;
+  uint32_t tail = 0;
+  if (packed && r.f) {
+    int32_t lastv = 0;
+    uint32_t lastlen = 0;
+#pragma unroll
+    for (int e = 0; e < DIR_ROWS; e++)
+      if (r.f >> e & 1u) {
+        lastv = r.v[e];
+        lastlen = rows - e;
+      }
+    for (uint64_t i = i0 + DIR_ROWS; i < n && lastlen + tail < 31u && rval[i] == lastv; i++) tail++;
+  }
 #pragma unroll
   for (int e = 0; e < DIR_ROWS; e++) {
     if (!(r.f >> e & 1u)) continue;
     const uint32_t hv = ej_hash32((uint32_t)r.v[e]);
     run = max(run, (long long)(hv >> shift) - (long long)k);
     const long long pos = (long long)k + run;
-    const uint2 entry = make_uint2(hv, (uint32_t)(i0 + e));
+    const uint32_t rest = r.f >> e >> 1;  // the thread's later keys
+    const uint32_t len = rest ? (uint32_t)__ffs(rest) : rows - e + tail;
+    const uint32_t y = packed ? (uint32_t)(i0 + e) << 5 | min(len, 31u) : (uint32_t)(i0 + e);
+    const uint2 entry = make_uint2(hv, y);
     // key 0's leading slots [0, pos_0) are written by dir_edges
     for (long long g = (k ? prev + 1 : pos); g <= pos; g++) dir[g] = entry;
-    if (k == 0) hdr->pos_first = (unsigned long long)pos;
+    if (k == 0) {
+      hdr->pos_first = (unsigned long long)pos;
+      hdr->lead = y;
+    }
     if (k + 1 == nk) hdr->pos_last = (unsigned long long)pos;
     prev = pos;
     k++;
@@ -188,16 +217,18 @@ __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval,
 
 // the slots before the first entry (copies of the first key) and from one
 // past the last entry to 2^bits + 1, at least two of them (sentinels
-// {0xFFFFFFFF, n}; a probe reads the slot after the one it stops at); with no
-// keys, slots [0, 2^bits + 1]; threads i0, i0 + stride, ... of the caller
+// {0xFFFFFFFF, n}, packed {0xFFFFFFFF, n << 5}; a probe may read the slot
+// after the one it stops at); with no keys, slots [0, 2^bits + 1]; threads
+// i0, i0 + stride, ... of the caller
 __device__ __forceinline__ void dir_edges(const DirHeader* __restrict__ hdr, uint64_t n, uint2* __restrict__ dir,
-                                          uint64_t i0, uint64_t stride) {
+                                          uint64_t i0, uint64_t stride, bool packed) {
   const unsigned long long home_end = 1ull << hdr->bits;
   const bool any = hdr->nkeys != 0;
   const unsigned long long first = any ? hdr->pos_first : 0ull;
   const unsigned long long tail = any ? hdr->pos_last + 1 : 0ull;
   const unsigned long long tail_end = max(home_end, tail) + 2;
-  const uint2 lead = make_uint2(hdr->hash0, 0u), sentinel = make_uint2(0xFFFFFFFFu, (uint32_t)n);
+  const uint2 lead = make_uint2(hdr->hash0, packed ? hdr->lead : 0u);
+  const uint2 sentinel = make_uint2(0xFFFFFFFFu, packed ? (uint32_t)n << 5 : (uint32_t)n);
   for (uint64_t i = i0; i < first; i += stride) dir[i] = lead;
   for (uint64_t i = tail + i0; i < tail_end; i += stride) dir[i] = sentinel;
 }

@@ -228,8 +228,9 @@ struct ej_table_view {
   const int32_t* rkey = nullptr;     // [nR + pad] row ids in table order
   const int32_t* rval = nullptr;     // [nR + pad] join keys in table order
   const uint2* bucket = nullptr;     // [2^hb] (hash, batched tables): row bounds of each bucket
-  const uint2* dir = nullptr;        // (hash, single tables) key directory {hash, run start}
+  const uint2* dir = nullptr;        // (hash, single tables) key directory {hash, run start [, length]}
   const uint32_t* dir_bits = nullptr;  // device word: the directory has 2^bits home slots
+  uint32_t dir_packed = 0;             // entries {hash, start << 5 | run length} (tables under 2^27 rows)
   const void* vbuckets = nullptr;    // (sorted) device EjValueBuckets {vmin, vmax, vshift} of `bucket`
   uint64_t nR = 0;
   uint32_t hb = 1;

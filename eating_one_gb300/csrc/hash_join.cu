@@ -120,15 +120,17 @@ __global__ void __launch_bounds__(1024) dir_prefix_kernel(const long long* __res
 __global__ void __launch_bounds__(DIR_THREADS) dir_place_kernel(const int32_t* __restrict__ rval, uint64_t n,
                                                                 const uint32_t* __restrict__ tile_off,
                                                                 const long long* __restrict__ kpre, DirHeader* hdr,
-                                                                uint2* __restrict__ dir) {
+                                                                uint2* __restrict__ dir, uint32_t packed) {
   if (hdr->bits == 0) return;  // bucket bounds instead
-  dir_tile_place(rval, n, (uint64_t)blockIdx.x * DIR_TILE, tile_off[blockIdx.x], kpre[blockIdx.x], hdr, dir);
+  dir_tile_place(rval, n, (uint64_t)blockIdx.x * DIR_TILE, tile_off[blockIdx.x], kpre[blockIdx.x], hdr, dir,
+                 packed != 0);
 }
 
 __global__ void __launch_bounds__(256) dir_edge_kernel(const DirHeader* __restrict__ hdr, uint64_t n,
-                                                       uint2* __restrict__ dir) {
+                                                       uint2* __restrict__ dir, uint32_t packed) {
   if (hdr->bits == 0) return;  // bucket bounds instead
-  dir_edges(hdr, n, dir, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
+  dir_edges(hdr, n, dir, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x,
+            packed != 0);
 }
 
 // bucket bounds of a table whose header chose them over the directory; a
@@ -203,7 +205,8 @@ probe_write_kernel(const ej_tuple* __restrict__ P, const void* __restrict__ desc
   if (w == 0 && threadIdx.x == 0 && woff[nwtiles] > cap) ej_set_status(st, EJ_ERR_CAPACITY, 0u);
   ej_prefetch_tile(P, w + ahead, nP, threadIdx.x & 31u);  // the tile a warp one resident wave later takes
   // the tile's descriptors: 1 KB (wide, lanes 8..15) or 512 bytes (packed, lanes 8..11)
-  if (DESC == EJ_DESC_PACKED) {
+  if (DESC == EJ_DESC_NONE) {
+  } else if (DESC == EJ_DESC_PACKED) {
     const unsigned l = (threadIdx.x & 31u) - 8u;
     const uint64_t doff = (w + ahead) * (PR_WTILE * 4) + (uint64_t)l * 128u;
     if (l < 4u && doff < nP * 4) asm volatile("prefetch.global.L2 [%0];" ::"l"(static_cast<const char*>(desc) + doff));
@@ -264,7 +267,7 @@ ej_status launch_count_w(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
   const uint64_t ahead = (uint64_t)h->num_sms * 40;  // warp tiles of one resident wave
   const dim3 grid((unsigned)pp.ntiles);
   constexpr int TH = WARPS * 32;
-  if (!desc)
+  if (!desc || desc_form(t) == EJ_DESC_NONE)
     probe_count_kernel<KIND, OUTER, EJ_DESC_NONE, WARPS><<<grid, TH, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles,
                                                                                      nullptr, ahead);
   else if (desc_form(t) == EJ_DESC_PACKED)
@@ -289,7 +292,10 @@ ej_status launch_write_w(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
   const uint64_t ahead = (uint64_t)h->num_sms * 32;  // warp tiles of one resident wave
   const dim3 grid((unsigned)pp.ntiles);
   constexpr int TH = WARPS * 32;
-  if (desc_form(t) == EJ_DESC_PACKED)
+  if (desc_form(t) == EJ_DESC_NONE)
+    probe_write_kernel<KIND, OUTER, EJ_DESC_NONE, WARPS><<<grid, TH, 0, h->stream>>>(
+        P, nullptr, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
+  else if (desc_form(t) == EJ_DESC_PACKED)
     probe_write_kernel<KIND, OUTER, EJ_DESC_PACKED, WARPS><<<grid, TH, 0, h->stream>>>(
         P, desc, pp.nP, t, woff, pp.nwtiles, out, cap, h->d_status, ahead);
   else
@@ -425,6 +431,7 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
     uint32_t* off = reinterpret_cast<uint32_t*>(ej_arena_at(h, tp.dir_off_off));
     long long* kmax = reinterpret_cast<long long*>(ej_arena_at(h, tp.dir_kmax_off));
     long long* kpre = reinterpret_cast<long long*>(ej_arena_at(h, tp.dir_kpre_off));
+    const uint32_t packed = tp.nR < (1ull << 27) ? 1u : 0u;  // start << 5 | run length fits 32 bits
     if (tiles) {
       dir_count_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, keys);
       EJ_TRY(ej_check_launch(h, "dir_count_kernel"));
@@ -433,19 +440,20 @@ ej_status ej_table_build(ej_handle* h, const ej_table_plan_t& tp, const ej_tuple
       EJ_TRY(ej_check_launch(h, "dir_tilemax_kernel"));
       dir_prefix_kernel<<<1, 1024, 0, h->stream>>>(kmax, tiles, kpre, hdr);
       EJ_TRY(ej_check_launch(h, "dir_prefix_kernel"));
-      dir_place_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, kpre, hdr, dir);
+      dir_place_kernel<<<tiles, 256, 0, h->stream>>>(rval, tp.nR, off, kpre, hdr, dir, packed);
       EJ_TRY(ej_check_launch(h, "dir_place_kernel"));
       const uint64_t bblocks = std::min<uint64_t>((tp.nR + 1 + 2047) / 2048, (uint64_t)h->num_sms * 8);
       dir_bucket_kernel<<<(unsigned)bblocks, 256, 0, h->stream>>>(rval, tp.nR, bucket, tp.hb, hdr);
       EJ_TRY(ej_check_launch(h, "dir_bucket_kernel"));
     } else {  // no rows: no keys, two home slots
-      const DirHeader empty = {1u, 0u, 0ull, 0ull, 0ull};
+      const DirHeader empty = {1u, 0u, 0ull, 0ull, 0ull, 0u, 0u};
       EJ_CUDA(h, cudaMemcpyAsync(hdr, &empty, sizeof empty, cudaMemcpyHostToDevice, h->stream));
     }
-    dir_edge_kernel<<<(unsigned)h->num_sms * 4, 256, 0, h->stream>>>(hdr, tp.nR, dir);
+    dir_edge_kernel<<<(unsigned)h->num_sms * 4, 256, 0, h->stream>>>(hdr, tp.nR, dir, packed);
     EJ_TRY(ej_check_launch(h, "dir_edge_kernel"));
     view->dir = dir;
     view->dir_bits = &hdr->bits;
+    view->dir_packed = packed;
     view->bucket = bucket;
   } else {  // sorted: value buckets, header first
     EjValueBuckets* vh = static_cast<EjValueBuckets*>(aux);

@@ -276,6 +276,50 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
                                                   uint32_t (&lo)[N], uint32_t (&c)[N]) {
   // a directory table whose build chose bucket bounds has bits = 0
   const uint32_t bits = t.dir ? __ldg(t.dir_bits) : 0u;
+  if (bits && t.dir_packed) {
+    // packed entries {hash, start << 5 | run length}: one 8-byte load of the
+    // home slot, more only past smaller hashes or for a run of 31 rows or
+    // more (its end is the next slot's start)
+    const uint32_t shift = 32u - bits;
+    uint32_t hv[N], slot[N];
+    uint2 a[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      hv[j] = ej_hash32((uint32_t)v[j]);
+      slot[j] = hv[j] >> shift;
+      a[j] = make_uint2(0u, 0u);
+      if (ok[j]) a[j] = __ldg(t.dir + slot[j]);
+    }
+    uint32_t walk = 0;
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      if (ok[j] && a[j].x < hv[j]) walk |= 1u << j;
+    while (walk) {
+#pragma unroll
+      for (int j = 0; j < N; j++)
+        if (walk & (1u << j)) a[j] = __ldg(t.dir + ++slot[j]);
+#pragma unroll
+      for (int j = 0; j < N; j++)
+        if ((walk & (1u << j)) && a[j].x >= hv[j]) walk &= ~(1u << j);
+    }
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      lo[j] = 0u;
+      c[j] = 0u;
+      const uint32_t start = a[j].y >> 5;
+      if (!ok[j] || a[j].x != hv[j] || start >= t.nR) continue;
+      lo[j] = start;
+      c[j] = a[j].y & 31u;
+      if (c[j] == 31u) {
+        // the walk stopped at the key's own slot, so the next slot starts the
+        // next run; the loop is a guard
+        uint32_t next = __ldg(t.dir + slot[j] + 1).y >> 5;
+        while (next == start) next = __ldg(t.dir + ++slot[j] + 1).y >> 5;
+        c[j] = next - start;
+      }
+    }
+    return;
+  }
   if (bits) {
     // key directory: every slot holds the first key at or after it; walk past
     // smaller hashes, then the run ends at the first slot with another start

@@ -280,7 +280,7 @@ __device__ __forceinline__ void ej_probe_write_warp(const ej_tuple* __restrict__
   EjProbeWarp w;
   bool escape = false;
 #pragma unroll
-  for (int j = 0; j < PR_ITEMS; j++) {
+  for (int j = 0; j < PR_ITEMS && DESC != EJ_DESC_NONE; j++) {
     const uint64_t idx = base + (uint64_t)j * 32 + lane;
     const bool ok = idx < nP;
     w.s[j] = ok ? __ldcs(reinterpret_cast<const int2*>(P) + idx) : make_int2(0, 0);
@@ -295,7 +295,10 @@ __device__ __forceinline__ void ej_probe_write_warp(const ej_tuple* __restrict__
       w.cnt[j] = d.y;
     }
   }
-  if (DESC == EJ_DESC_PACKED && __any_sync(EJ_FULL_MASK, escape)) ej_probe_runs_warp<KIND, OUTER>(P, base, nP, t, w);
+  // no descriptors (a packed key directory answers a probe in one load): the
+  // count pass's find, repeated
+  if (DESC == EJ_DESC_NONE || (DESC == EJ_DESC_PACKED && __any_sync(EJ_FULL_MASK, escape)))
+    ej_probe_runs_warp<KIND, OUTER>(P, base, nP, t, w);
   int32_t kk[PR_ITEMS][PW_PREFETCH];
   ej_probe_prefetch(t, w, kk);
   ej_emit_warp(w, kk, t, off, out, cap, stage);
