@@ -3,10 +3,13 @@
 // batch (batch.cu).
 //
 // The distinct keys of the hash-sorted table, in hash order, each an entry
-// {hash, run start} placed by linear probing from its home slot
-// hash >> (32 - bits), 2^bits >= 2 x keys: key k goes to
+// {hash, run start} placed by linear probing from its home slot, the even
+// slot (hash >> (32 - bits)) & ~1 (2^bits >= 4 x keys where the reserved
+// slots allow, else as many as they hold): key k goes to
 //   pos_k = max(home_k, pos_{k-1} + 1) = k + max_{j <= k} (home_j - j),
-// so the entries stay in hash order.  Tables under 2^27 rows pack an entry
+// so the entries stay in hash order.  A probe loads the aligned 16-byte pair
+// of slots at its home, so that it needs a second load only when both hold
+// smaller hashes (about 4% of probes at a quarter of the slots filled).  Tables under 2^27 rows pack an entry
 // as {hash, start << 5 | run length} (31: 31 rows or more, the run then ends
 // at the next slot's start), so that one 8-byte load answers most probes;
 // larger tables keep {hash, start}.  Every slot holds the first key at or
@@ -87,11 +90,16 @@ __device__ __forceinline__ void dir_rows(const int32_t* __restrict__ rval, uint6
   }
 }
 
-__device__ __forceinline__ uint32_t dir_bits_for(unsigned long long nk) {
+// bits of a directory of nk keys in a table of n rows: 2^bits >= 4 nk, at most
+// the power of two ej_dir_capacity(n) reserves (>= 2 n >= 2 nk)
+__device__ __forceinline__ uint32_t dir_bits_for(unsigned long long nk, unsigned long long n) {
   uint32_t bits = 1;
-  while (bits < 32 && (1ull << bits) < 2 * nk) bits++;
+  while (bits < 32 && (1ull << bits) < 4 * nk && (1ull << bits) < 2 * n) bits++;
   return bits;
 }
+
+// home slot of a hash: even, so that its pair is one aligned 16-byte load
+__device__ __forceinline__ uint32_t dir_home(uint32_t hv, uint32_t shift) { return (hv >> shift) & ~1u; }
 
 // block-wide maximum scan, exclusive (LLONG_MIN for thread 0); *total = the block maximum
 __device__ __forceinline__ long long dir_block_exclusive_max(long long v, long long* tmp, long long* total) {
@@ -141,7 +149,7 @@ __device__ __forceinline__ long long dir_tile_max(const int32_t* __restrict__ rv
 #pragma unroll
   for (int e = 0; e < DIR_ROWS; e++)
     if (r.f >> e & 1u) {
-      m = max(m, (long long)(ej_hash32((uint32_t)r.v[e]) >> shift) - (long long)k);
+      m = max(m, (long long)dir_home(ej_hash32((uint32_t)r.v[e]), shift) - (long long)k);
       k++;
     }
   if (row0 == 0 && threadIdx.x == 0) *hash0 = ej_hash32((uint32_t)r.v[0]);  // row 0 begins the first key
@@ -171,7 +179,7 @@ __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval,
 #pragma unroll
   for (int e = 0; e < DIR_ROWS; e++)
     if (r.f >> e & 1u) {
-      m = max(m, (long long)(ej_hash32((uint32_t)r.v[e]) >> shift) - (long long)kk);
+      m = max(m, (long long)dir_home(ej_hash32((uint32_t)r.v[e]), shift) - (long long)kk);
       kk++;
     }
   long long all;
@@ -197,7 +205,7 @@ __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval,
   for (int e = 0; e < DIR_ROWS; e++) {
     if (!(r.f >> e & 1u)) continue;
     const uint32_t hv = ej_hash32((uint32_t)r.v[e]);
-    run = max(run, (long long)(hv >> shift) - (long long)k);
+    run = max(run, (long long)dir_home(hv, shift) - (long long)k);
     const long long pos = (long long)k + run;
     const uint32_t rest = r.f >> e >> 1;  // the thread's later keys
     const uint32_t len = rest ? (uint32_t)__ffs(rest) : rows - e + tail;

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(DIR_THREADS) dir_tilemax_kernel(const int32_t*
     }
     return;
   }
-  const uint32_t bits = dir_bits_for(nk);
+  const uint32_t bits = dir_bits_for(nk, n);
   const long long m = dir_tile_max(rval, n, (uint64_t)blockIdx.x * DIR_TILE, tile_off[blockIdx.x], bits, &hdr->hash0);
   if (threadIdx.x == 0) kmax[blockIdx.x] = m;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -193,6 +193,86 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
   if ((threadIdx.x & 31u) == 0) wcount[w] = total;
 }
 
+// Count pass over a packed key directory (inner join, hash table), lean: a
+// directory entry {hash, start << 5 | run length} is already the packed run
+// descriptor of the write pass (escape 31 included), so a probe costs its
+// hash, one 16-byte load of its home pair of slots (more only past smaller
+// hashes, or for a run of 31 rows or more) and the store of the entry's
+// second word.  Each warp takes
+// two 128-probe tiles, 8 probes per lane loaded two at a time (16-byte
+// loads), so that twice the directory loads are in flight per warp.  Tiles
+// that are not full (the last warp's) and tables whose build chose bucket
+// bounds (bits = 0 in the header) take the general path.  STORE: the
+// descriptors are kept for the write pass.
+constexpr int PCD_TILES = 2;  // warp tiles per warp
+
+template <bool STORE>
+__global__ void __launch_bounds__(256, 4)
+probe_count_dir_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
+                       unsigned long long* __restrict__ wcount, uint64_t nwtiles, uint32_t* __restrict__ desc,
+                       uint64_t ahead) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint64_t w0 = ((uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * PCD_TILES;
+  if (w0 >= nwtiles) return;
+  {  // the two tiles a warp one resident wave later takes: 2 KB, lanes 0..15
+    const uint64_t off = (w0 + ahead) * (PR_WTILE * 8) + (uint64_t)lane * 128u;
+    if (lane < 16u && off < nP * 8) asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char*>(P) + off));
+  }
+  const uint32_t bits = __ldg(t.dir_bits);
+  const uint64_t base = w0 * PR_WTILE;
+  if (bits == 0 || base + PCD_TILES * PR_WTILE > nP) {
+    for (int k = 0; k < PCD_TILES; k++) {
+      const uint64_t w = w0 + k;
+      if (w >= nwtiles) break;
+      const unsigned long long total =
+          STORE ? ej_probe_count_warp_desc<EJ_TABLE_HASH, false, EJ_DESC_PACKED>(P, w * PR_WTILE, nP, t, desc)
+                : ej_probe_count_warp_desc<EJ_TABLE_HASH, false, EJ_DESC_NONE>(P, w * PR_WTILE, nP, t, nullptr);
+      if (lane == 0) wcount[w] = total;
+    }
+    return;
+  }
+  constexpr int N = 4 * PCD_TILES;  // probes per lane: 2 + 2j + {0, 1} of 64-probe half tile j
+  const uint32_t end = (uint32_t)t.nR << 5;  // entries at or past it: no key (sentinels)
+  // probe 2q + e of the lane sits at P[base + 64 q + 2 lane + e]
+  const int4* P4 = reinterpret_cast<const int4*>(P + base) + lane;
+  uint32_t hv[N], slot[N];
+  bool ok[N], hasb[N];
+  uint2 a[N], b[N];
+#pragma unroll
+  for (int q = 0; q < N / 2; q++) {
+    const int4 x = __ldcs(P4 + 32 * q);
+    hv[2 * q] = ej_hash32((uint32_t)x.y);
+    hv[2 * q + 1] = ej_hash32((uint32_t)x.w);
+    ok[2 * q] = ok[2 * q + 1] = true;
+  }
+  ej_dir_walk<N>(t.dir, 32u - bits, hv, ok, a, b, hasb, slot);
+  uint32_t d[N], sum[PCD_TILES] = {};
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    d[j] = (a[j].x == hv[j] && a[j].y < end) ? a[j].y : 0u;
+    uint32_t c = d[j] & 31u;
+    if (c == 31u) {  // 31 rows or more: the next slot starts the next run
+      const uint32_t start = d[j] >> 5;
+      uint32_t next = (hasb[j] ? b[j] : __ldg(t.dir + slot[j] + 1)).y >> 5;
+      while (next == start) next = __ldg(t.dir + ++slot[j] + 1).y >> 5;  // a guard
+      c = next - start;
+    }
+    sum[j / 4] += c;  // a lane's runs: under 4 x 2^27 rows per tile
+  }
+  if (STORE) {
+    uint2* D2 = reinterpret_cast<uint2*>(desc + base) + lane;
+#pragma unroll
+    for (int q = 0; q < N / 2; q++) __stcs(D2 + 32 * q, make_uint2(d[2 * q], d[2 * q + 1]));
+  }
+#pragma unroll
+  for (int k = 0; k < PCD_TILES; k++) {
+    // the tile's rows (under 2^34): 32-bit sums of the lanes' 16-bit halves
+    const uint32_t lo16 = __reduce_add_sync(EJ_FULL_MASK, sum[k] & 0xFFFFu);
+    const uint32_t hi16 = __reduce_add_sync(EJ_FULL_MASK, sum[k] >> 16);
+    if (lane == 0) wcount[w0 + k] = ((unsigned long long)hi16 << 16) + lo16;
+  }
+}
+
 template <int KIND, bool OUTER, int DESC, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32)
 probe_write_kernel(const ej_tuple* __restrict__ P, const void* __restrict__ desc, uint64_t nP, ej_table_view t,
@@ -267,6 +347,20 @@ ej_status launch_count_w(ej_handle* h, const ej_probe_plan_t& pp, const ej_tuple
   const uint64_t ahead = (uint64_t)h->num_sms * 40;  // warp tiles of one resident wave
   const dim3 grid((unsigned)pp.ntiles);
   constexpr int TH = WARPS * 32;
+  // inner probes of a packed key directory, 16-byte aligned: the lean count
+  // (8 warps of two tiles per block, 4 blocks per SM)
+  if (KIND == EJ_TABLE_HASH && !OUTER && t.dir && t.dir_packed && (reinterpret_cast<uintptr_t>(P) & 15u) == 0 &&
+      (!desc || desc_form(t) == EJ_DESC_PACKED)) {
+    const uint64_t blocks = (pp.nwtiles + 8 * PCD_TILES - 1) / (8 * PCD_TILES);
+    const uint64_t ahead2 = (uint64_t)h->num_sms * 4 * 8 * PCD_TILES;  // warp tiles of one resident wave
+    if (desc)
+      probe_count_dir_kernel<true><<<(unsigned)blocks, 256, 0, h->stream>>>(
+          P, pp.nP, t, wcount, pp.nwtiles, static_cast<uint32_t*>(desc), ahead2);
+    else
+      probe_count_dir_kernel<false><<<(unsigned)blocks, 256, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles,
+                                                                              nullptr, ahead2);
+    return ej_check_launch(h, "probe_count_dir_kernel");
+  }
   if (!desc || desc_form(t) == EJ_DESC_NONE)
     probe_count_kernel<KIND, OUTER, EJ_DESC_NONE, WARPS><<<grid, TH, 0, h->stream>>>(P, pp.nP, t, wcount, pp.nwtiles,
                                                                                      nullptr, ahead);

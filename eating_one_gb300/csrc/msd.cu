@@ -128,20 +128,29 @@ struct LsSmem {
 
 // exclusive sum in place of the LS_DIGITS counters c[0..] (c[LS_DIGITS] =
 // total); every thread, LS_DIGITS / LS_THREADS consecutive counters each
+// (16-byte loads and stores: c is 16-byte aligned; the counters are read
+// twice rather than held, as the caller's rows occupy the registers)
 __device__ __forceinline__ void ls_scan_digits(uint32_t* c, uint32_t* warp_tmp) {
-  constexpr int PER = LS_DIGITS / LS_THREADS;
-  uint32_t v[PER], sum = 0;
+  constexpr int PER4 = LS_DIGITS / LS_THREADS / 4;
+  uint4* c4 = reinterpret_cast<uint4*>(c) + threadIdx.x * PER4;
+  uint32_t sum = 0;
 #pragma unroll
-  for (int i = 0; i < PER; i++) {
-    v[i] = c[threadIdx.x * PER + i];
-    sum += v[i];
+  for (int i = 0; i < PER4; i++) {
+    const uint4 v = c4[i];
+    sum += v.x + v.y + v.z + v.w;
   }
   uint32_t total;
   uint32_t run = ej_block_exclusive_sum<LS_THREADS, uint32_t>(sum, warp_tmp, &total);
 #pragma unroll
-  for (int i = 0; i < PER; i++) {
-    c[threadIdx.x * PER + i] = run;
-    run += v[i];
+  for (int i = 0; i < PER4; i++) {
+    const uint4 v = c4[i];
+    uint4 o;
+    o.x = run;
+    o.y = o.x + v.x;
+    o.z = o.y + v.y;
+    o.w = o.z + v.z;
+    run = o.w + v.w;
+    c4[i] = o;
   }
   if (threadIdx.x == 0) c[LS_DIGITS] = total;
   __syncthreads();
@@ -221,33 +230,43 @@ __device__ void ls_bucket_global(LsSmem& sm, const ej_tuple* __restrict__ in, ej
 // (or the same hash and an earlier slot), so each row is written once, at
 // its final position.  Long sub-buckets (many rows of few keys) are sorted
 // by the whole CTA instead: a counting sort by their remaining bits.
+//
+// PER: row slots per thread (m <= PER * LS_THREADS), so that a small group
+// does not pay for the slots of the largest; up to 9 slots the rows' hashes
+// stay in registers between the ranking and the placement (beyond that they
+// are computed again, for want of registers).
+template <int PER>
 __device__ void ls_sort_smem(LsSmem& sm, const ej_tuple* __restrict__ in, uint64_t lo, uint32_t m,
                              uint32_t low_bits, int32_t* __restrict__ rkey, int32_t* __restrict__ rval) {
+  constexpr bool KEEP = PER <= 9;
   const unsigned t = threadIdx.x;
   const uint32_t sh = low_bits - LS_DIGIT_BITS;  // bits under the digit
-  for (uint32_t i = t; i < LS_DIGITS; i += LS_THREADS) sm.cnt[i] = 0;
+  for (uint32_t i = t; i < LS_DIGITS / 4; i += LS_THREADS) reinterpret_cast<uint4*>(sm.cnt)[i] = make_uint4(0, 0, 0, 0);
   if (t == 0) sm.nbig = 0;
   __syncthreads();
   // 1. rows into registers (coalesced), ranked within their digit
   const uint2* src = reinterpret_cast<const uint2*>(in) + lo;
-  uint2 v[LS_PER];
-  uint32_t rk[LS_PER];
+  uint2 v[PER];
+  uint32_t rk[PER], hk[KEEP ? PER : 1];
 #pragma unroll
-  for (int i = 0; i < LS_PER; i++) {
+  for (int i = 0; i < PER; i++) {
     const uint32_t j = t + (uint32_t)i * LS_THREADS;
     if (j < m) v[i] = __ldcs(src + j);
   }
 #pragma unroll
-  for (int i = 0; i < LS_PER; i++)
-    if (t + (uint32_t)i * LS_THREADS < m)
-      rk[i] = atomicAdd(&sm.cnt[(ej_hash32(v[i].y) >> sh) & (LS_DIGITS - 1)], 1u);
+  for (int i = 0; i < PER; i++)
+    if (t + (uint32_t)i * LS_THREADS < m) {
+      const uint32_t hv = ej_hash32(v[i].y);
+      if (KEEP) hk[KEEP ? i : 0] = hv;
+      rk[i] = atomicAdd(&sm.cnt[(hv >> sh) & (LS_DIGITS - 1)], 1u);
+    }
   __syncthreads();
   ls_scan_digits(sm.cnt, sm.warp_tmp);
   // 2. every row to its digit's sub-bucket
 #pragma unroll
-  for (int i = 0; i < LS_PER; i++)
+  for (int i = 0; i < PER; i++)
     if (t + (uint32_t)i * LS_THREADS < m) {
-      const uint32_t hv = ej_hash32(v[i].y);
+      const uint32_t hv = KEEP ? hk[KEEP ? i : 0] : ej_hash32(v[i].y);
       const uint32_t p = sm.cnt[(hv >> sh) & (LS_DIGITS - 1)] + rk[i];
       sm.row[p] = v[i];
       sm.hsh[p] = hv;
@@ -300,6 +319,21 @@ __device__ void ls_sort_smem(LsSmem& sm, const ej_tuple* __restrict__ in, uint64
   __syncthreads();  // shared memory is reused by the caller's next range
 }
 
+// ls_sort_smem with the fewest row slots per thread that hold m rows (groups
+// aim at LS_ROWS = 8 slots' worth; 9 takes most of those a little over)
+__device__ __forceinline__ void ls_sort_rows(LsSmem& sm, const ej_tuple* __restrict__ in, uint64_t lo, uint32_t m,
+                                             uint32_t low_bits, int32_t* __restrict__ rkey,
+                                             int32_t* __restrict__ rval) {
+  if (m <= 4u * LS_THREADS)
+    ls_sort_smem<4>(sm, in, lo, m, low_bits, rkey, rval);
+  else if (m <= 8u * LS_THREADS)
+    ls_sort_smem<8>(sm, in, lo, m, low_bits, rkey, rval);
+  else if (m <= 9u * LS_THREADS)
+    ls_sort_smem<9>(sm, in, lo, m, low_bits, rkey, rval);
+  else
+    ls_sort_smem<LS_PER>(sm, in, lo, m, low_bits, rkey, rval);
+}
+
 // One CTA per group of 2^g consecutive buckets (b = top 16 hash bits), whose
 // rows [bstart[b0], bstart[b0 + 2^g]) of `in` share hash bits 16 + g .. 31:
 // into the columns ordered by the full hash.  A group larger than shared
@@ -316,7 +350,7 @@ msd_local_kernel(const ej_tuple* __restrict__ in, ej_tuple* __restrict__ tmp, co
   const uint32_t lo = min(bstart[b0], n);
   const uint32_t hi = max(min(bstart[b1], n), lo);
   if (hi - lo <= (uint32_t)LS_CAP) {
-    if (hi > lo) ls_sort_smem(sm, in, lo, hi - lo, MSD_BUCKET_BITS + g, rkey, rval);
+    if (hi > lo) ls_sort_rows(sm, in, lo, hi - lo, MSD_BUCKET_BITS + g, rkey, rval);
     return;
   }
   for (uint32_t b = b0; b < b1; b++) {
@@ -325,7 +359,7 @@ msd_local_kernel(const ej_tuple* __restrict__ in, ej_tuple* __restrict__ tmp, co
     if (bhi - blo > (uint32_t)LS_CAP)
       ls_bucket_global(sm, in, tmp, blo, bhi - blo, rkey, rval);
     else if (bhi > blo)
-      ls_sort_smem(sm, in, blo, bhi - blo, MSD_BUCKET_BITS, rkey, rval);
+      ls_sort_rows(sm, in, blo, bhi - blo, MSD_BUCKET_BITS, rkey, rval);
   }
 }
 

@@ -268,6 +268,55 @@ __device__ __forceinline__ void ej_find_runs_bucket(const ej_table_view& t, cons
   for (int j = 0; j < N; j++) lo[j] -= t.voff;
 }
 
+// The key directory's slots of N probe hashes (dir.cuh): every probe loads
+// the aligned 16-byte pair at its even home slot (hv >> shift) & ~1, then the
+// next pair while both slots hold smaller hashes (slots are in hash order, so
+// the second is the larger); the N walks advance together, one pair per
+// round, so that a warp waits for as many dependent loads as its longest
+// walk.  Out: a[j] the entry of the first slot whose hash is hv[j] or more,
+// slot[j] that slot; when hasb[j], b[j] is the entry of the slot after it
+// (else it is left to the caller to load).  ok[j] false: a[j].x = 0xFFFFFFFF.
+template <int N>
+__device__ __forceinline__ void ej_dir_walk(const uint2* __restrict__ dir, uint32_t shift, const uint32_t (&hv)[N],
+                                            const bool (&ok)[N], uint2 (&a)[N], uint2 (&b)[N], bool (&hasb)[N],
+                                            uint32_t (&slot)[N]) {
+  const uint4* d4 = reinterpret_cast<const uint4*>(dir);  // 16-byte aligned
+  uint4 q[N];
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    slot[j] = (hv[j] >> shift) & ~1u;
+    q[j] = make_uint4(0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u);
+    if (ok[j]) q[j] = __ldg(d4 + (slot[j] >> 1));
+  }
+  uint32_t walk = 0;
+#pragma unroll
+  for (int j = 0; j < N; j++)
+    if (q[j].z < hv[j]) walk |= 1u << j;
+  while (walk) {  // the sentinels after the last entry end every walk
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      if (walk & (1u << j)) {
+        slot[j] += 2;
+        q[j] = __ldg(d4 + (slot[j] >> 1));
+      }
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      if ((walk & (1u << j)) && q[j].z >= hv[j]) walk &= ~(1u << j);
+  }
+#pragma unroll
+  for (int j = 0; j < N; j++) {
+    hasb[j] = q[j].x >= hv[j];
+    if (hasb[j]) {
+      a[j] = make_uint2(q[j].x, q[j].y);
+      b[j] = make_uint2(q[j].z, q[j].w);
+    } else {
+      a[j] = make_uint2(q[j].z, q[j].w);
+      b[j] = a[j];
+      slot[j] += 1;
+    }
+  }
+}
+
 // Runs of N probe values of a hash table at once: through the key directory
 // (single tables that carry one), else through bucket bounds.  ok[j] false:
 // c[j] = 0.
@@ -276,104 +325,45 @@ __device__ __forceinline__ void ej_find_runs_hash(const ej_table_view& t, const 
                                                   uint32_t (&lo)[N], uint32_t (&c)[N]) {
   // a directory table whose build chose bucket bounds has bits = 0
   const uint32_t bits = t.dir ? __ldg(t.dir_bits) : 0u;
-  if (bits && t.dir_packed) {
-    // packed entries {hash, start << 5 | run length}: one 8-byte load of the
-    // home slot, more only past smaller hashes or for a run of 31 rows or
-    // more (its end is the next slot's start)
-    const uint32_t shift = 32u - bits;
-    uint32_t hv[N], slot[N];
-    uint2 a[N];
-#pragma unroll
-    for (int j = 0; j < N; j++) {
-      hv[j] = ej_hash32((uint32_t)v[j]);
-      slot[j] = hv[j] >> shift;
-      a[j] = make_uint2(0u, 0u);
-      if (ok[j]) a[j] = __ldg(t.dir + slot[j]);
-    }
-    uint32_t walk = 0;
-#pragma unroll
-    for (int j = 0; j < N; j++)
-      if (ok[j] && a[j].x < hv[j]) walk |= 1u << j;
-    while (walk) {
-#pragma unroll
-      for (int j = 0; j < N; j++)
-        if (walk & (1u << j)) a[j] = __ldg(t.dir + ++slot[j]);
-#pragma unroll
-      for (int j = 0; j < N; j++)
-        if ((walk & (1u << j)) && a[j].x >= hv[j]) walk &= ~(1u << j);
-    }
-#pragma unroll
-    for (int j = 0; j < N; j++) {
-      lo[j] = 0u;
-      c[j] = 0u;
-      const uint32_t start = a[j].y >> 5;
-      if (!ok[j] || a[j].x != hv[j] || start >= t.nR) continue;
-      lo[j] = start;
-      c[j] = a[j].y & 31u;
-      if (c[j] == 31u) {
-        // the walk stopped at the key's own slot, so the next slot starts the
-        // next run; the loop is a guard
-        uint32_t next = __ldg(t.dir + slot[j] + 1).y >> 5;
-        while (next == start) next = __ldg(t.dir + ++slot[j] + 1).y >> 5;
-        c[j] = next - start;
-      }
-    }
-    return;
-  }
   if (bits) {
-    // key directory: every slot holds the first key at or after it; walk past
-    // smaller hashes, then the run ends at the first slot with another start
-    // (slot + 1 never passes the sentinels after the last entry)
-    const uint32_t shift = 32u - bits;
+    // key directory: every slot holds the first key at or after it; a present
+    // key's walk stops at its own slot, and the slot after it starts the next
+    // run (the loops that look further are guards)
     uint32_t hv[N], slot[N];
     uint2 a[N], b[N];
+    bool hasb[N];
 #pragma unroll
-    for (int j = 0; j < N; j++) {
-      hv[j] = ej_hash32((uint32_t)v[j]);
-      slot[j] = hv[j] >> shift;
-      a[j] = b[j] = make_uint2(0u, 0u);
-      if (ok[j]) {
-        // the home slot and the next: one 16-byte load of the aligned pair
-        // when the home slot is even (the directory starts 16-byte aligned),
-        // else two 8-byte loads (the L1 data path pays for the bytes it
-        // delivers, and the pair holding an odd slot brings one not needed)
-        if (slot[j] & 1u) {
-          a[j] = __ldg(t.dir + slot[j]);
-          b[j] = __ldg(t.dir + slot[j] + 1);
-        } else {
-          const uint4 q = __ldg(reinterpret_cast<const uint4*>(t.dir) + (slot[j] >> 1));
-          a[j] = make_uint2(q.x, q.y);
-          b[j] = make_uint2(q.z, q.w);
+    for (int j = 0; j < N; j++) hv[j] = ej_hash32((uint32_t)v[j]);
+    ej_dir_walk<N>(t.dir, 32u - bits, hv, ok, a, b, hasb, slot);
+    if (t.dir_packed) {
+      // packed entries {hash, start << 5 | run length}: the length is in
+      // hand unless the run has 31 rows or more (its end: the next start)
+#pragma unroll
+      for (int j = 0; j < N; j++) {
+        lo[j] = 0u;
+        c[j] = 0u;
+        const uint32_t start = a[j].y >> 5;
+        if (!ok[j] || a[j].x != hv[j] || start >= t.nR) continue;
+        lo[j] = start;
+        c[j] = a[j].y & 31u;
+        if (c[j] == 31u) {
+          uint32_t next = (hasb[j] ? b[j] : __ldg(t.dir + slot[j] + 1)).y >> 5;
+          while (next == start) next = __ldg(t.dir + ++slot[j] + 1).y >> 5;
+          c[j] = next - start;
         }
       }
-    }
-    // the N walks advance together, one slot per round, so that a warp waits
-    // for as many dependent loads as its longest walk, not for their sum
-    uint32_t walk = 0;
+    } else {
+      // {hash, start}: the run ends at the next slot's start
 #pragma unroll
-    for (int j = 0; j < N; j++)
-      if (ok[j] && a[j].x < hv[j]) walk |= 1u << j;
-    while (walk) {
-#pragma unroll
-      for (int j = 0; j < N; j++)
-        if (walk & (1u << j)) {
-          a[j] = b[j];
-          b[j] = __ldg(t.dir + ++slot[j] + 1);
-        }
-#pragma unroll
-      for (int j = 0; j < N; j++)
-        if ((walk & (1u << j)) && a[j].x >= hv[j]) walk &= ~(1u << j);
-    }
-#pragma unroll
-    for (int j = 0; j < N; j++) {
-      lo[j] = 0u;
-      c[j] = 0u;
-      if (!ok[j] || a[j].x != hv[j] || a[j].y >= t.nR) continue;
-      // a present key's home slot is never a gap, so the walk stops at the
-      // key's own slot and the next slot starts another run; the loop is a guard
-      while (b[j].y == a[j].y) b[j] = __ldg(t.dir + ++slot[j] + 1);
-      lo[j] = a[j].y;
-      c[j] = b[j].y - a[j].y;
+      for (int j = 0; j < N; j++) {
+        lo[j] = 0u;
+        c[j] = 0u;
+        if (!ok[j] || a[j].x != hv[j] || a[j].y >= t.nR) continue;
+        uint2 nb = hasb[j] ? b[j] : __ldg(t.dir + slot[j] + 1);
+        while (nb.y == a[j].y) nb = __ldg(t.dir + ++slot[j] + 1);
+        lo[j] = a[j].y;
+        c[j] = nb.y - a[j].y;
+      }
     }
     return;
   }
