@@ -126,31 +126,31 @@ struct LsSmem {
   uint32_t nbig;
 };
 
-// exclusive sum in place of the LS_DIGITS counters c[0..] (c[LS_DIGITS] =
-// total); every thread, LS_DIGITS / LS_THREADS consecutive counters each
-// (16-byte loads and stores: c is 16-byte aligned; the counters are read
-// twice rather than held, as the caller's rows occupy the registers)
+// Digit d's counter sits at ls_at(d) = d ^ ((d >> 5) & 31), a permutation
+// within each 32-counter row: the scan below, where thread t takes digits
+// 16t .. 16t + 15, and the placement, where a warp's lanes take consecutive
+// rows of non-decreasing digits, both read 32 distinct banks per instruction
+// (a plain layout gave the scan 16-way conflicts).  Index LS_DIGITS (the
+// total) maps to itself.
+__device__ __forceinline__ uint32_t ls_at(uint32_t d) { return d ^ ((d >> 5) & 31u); }
+
+// exclusive sum in place of the LS_DIGITS counters (at ls_at(d)); c at
+// LS_DIGITS = total.  Every thread, LS_DIGITS / LS_THREADS consecutive
+// digits; the counters are read twice rather than held, as the caller's rows
+// occupy the registers
 __device__ __forceinline__ void ls_scan_digits(uint32_t* c, uint32_t* warp_tmp) {
-  constexpr int PER4 = LS_DIGITS / LS_THREADS / 4;
-  uint4* c4 = reinterpret_cast<uint4*>(c) + threadIdx.x * PER4;
+  constexpr int PER = LS_DIGITS / LS_THREADS;
+  const uint32_t d0 = threadIdx.x * PER;
   uint32_t sum = 0;
 #pragma unroll
-  for (int i = 0; i < PER4; i++) {
-    const uint4 v = c4[i];
-    sum += v.x + v.y + v.z + v.w;
-  }
+  for (int i = 0; i < PER; i++) sum += c[ls_at(d0 + i)];
   uint32_t total;
   uint32_t run = ej_block_exclusive_sum<LS_THREADS, uint32_t>(sum, warp_tmp, &total);
 #pragma unroll
-  for (int i = 0; i < PER4; i++) {
-    const uint4 v = c4[i];
-    uint4 o;
-    o.x = run;
-    o.y = o.x + v.x;
-    o.z = o.y + v.y;
-    o.w = o.z + v.z;
-    run = o.w + v.w;
-    c4[i] = o;
+  for (int i = 0; i < PER; i++) {
+    const uint32_t x = c[ls_at(d0 + i)];
+    c[ls_at(d0 + i)] = run;
+    run += x;
   }
   if (threadIdx.x == 0) c[LS_DIGITS] = total;
   __syncthreads();
@@ -258,7 +258,7 @@ __device__ void ls_sort_smem(LsSmem& sm, const ej_tuple* __restrict__ in, uint64
     if (t + (uint32_t)i * LS_THREADS < m) {
       const uint32_t hv = ej_hash32(v[i].y);
       if (KEEP) hk[KEEP ? i : 0] = hv;
-      rk[i] = atomicAdd(&sm.cnt[(hv >> sh) & (LS_DIGITS - 1)], 1u);
+      rk[i] = atomicAdd(&sm.cnt[ls_at((hv >> sh) & (LS_DIGITS - 1))], 1u);
     }
   __syncthreads();
   ls_scan_digits(sm.cnt, sm.warp_tmp);
@@ -267,7 +267,7 @@ __device__ void ls_sort_smem(LsSmem& sm, const ej_tuple* __restrict__ in, uint64
   for (int i = 0; i < PER; i++)
     if (t + (uint32_t)i * LS_THREADS < m) {
       const uint32_t hv = KEEP ? hk[KEEP ? i : 0] : ej_hash32(v[i].y);
-      const uint32_t p = sm.cnt[(hv >> sh) & (LS_DIGITS - 1)] + rk[i];
+      const uint32_t p = sm.cnt[ls_at((hv >> sh) & (LS_DIGITS - 1))] + rk[i];
       sm.row[p] = v[i];
       sm.hsh[p] = hv;
     }
@@ -278,7 +278,7 @@ __device__ void ls_sort_smem(LsSmem& sm, const ej_tuple* __restrict__ in, uint64
   for (uint32_t p = t; p < m; p += LS_THREADS) {
     const uint32_t hv = sm.hsh[p];
     const uint32_t d = (hv >> sh) & (LS_DIGITS - 1);
-    const uint32_t a = sm.cnt[d], e = sm.cnt[d + 1];
+    const uint32_t a = sm.cnt[ls_at(d)], e = sm.cnt[ls_at(d + 1)];
     if (e - a > LS_SMALL) {
       if (p == a) sm.big[atomicAdd(&sm.nbig, 1u)] = d;
       continue;
@@ -298,7 +298,7 @@ __device__ void ls_sort_smem(LsSmem& sm, const ej_tuple* __restrict__ in, uint64
   const uint32_t nbig = sm.nbig, rmask = (1u << sh) - 1u;
   for (uint32_t q = 0; q < nbig; q++) {
     const uint32_t d = sm.big[q];
-    const uint32_t a = sm.cnt[d], len = sm.cnt[d + 1] - a;
+    const uint32_t a = sm.cnt[ls_at(d)], len = sm.cnt[ls_at(d + 1)] - a;
     sm.cnt2[t] = 0;
     __syncthreads();
     for (uint32_t j = t; j < len; j += LS_THREADS) atomicAdd(&sm.cnt2[sm.hsh[a + j] & rmask], 1u);
