@@ -63,26 +63,30 @@ __device__ __forceinline__ void dir_rows(const int32_t* __restrict__ rval, uint6
 #pragma unroll
   for (int e = 0; e < DIR_ROWS; e++) r.v[e] = 0;
   if (i0 >= n) return;
-  // 16-byte loads of the aligned chunks holding the thread's rows: a batched
-  // table's rows start anywhere in the shared column, so the first row may sit
-  // m = 1..3 ints past a chunk boundary.  A chunk is loaded only when it
-  // starts before row n, so the loads stay inside the column (padded by 8 rows).
-  const uint32_t m = (uint32_t)(reinterpret_cast<uintptr_t>(rval + i0) >> 2) & 3u;
-  const int4* c4 = reinterpret_cast<const int4*>(rval + i0 - m);
-  int32_t w[DIR_ROWS + 4];
-#pragma unroll
-  for (int q = 0; q < DIR_ROWS / 4 + 1; q++) {
-    int4 x = make_int4(0, 0, 0, 0);
-    if (i0 + 4u * q < n + m) x = c4[q];
-    w[4 * q] = x.x;
-    w[4 * q + 1] = x.y;
-    w[4 * q + 2] = x.z;
-    w[4 * q + 3] = x.w;
-  }
-#pragma unroll
-  for (int e = 0; e < DIR_ROWS; e++)  // w[e + m], static indices only
-    r.v[e] = m == 0 ? w[e] : m == 1 ? w[e + 1] : m == 2 ? w[e + 2] : w[e + 3];
   int32_t prev = i0 ? rval[i0 - 1] : 0;
+  if (i0 + DIR_ROWS <= n && (reinterpret_cast<uintptr_t>(rval + i0) & 15u) == 0) {
+    // a full run of rows at a 16-byte boundary (the columns start aligned
+    // and tiles begin at multiples of DIR_ROWS rows): four 16-byte loads
+    const int4* c4 = reinterpret_cast<const int4*>(rval + i0);
+#pragma unroll
+    for (int q = 0; q < DIR_ROWS / 4; q++) {
+      const int4 x = c4[q];
+      r.v[4 * q] = x.x;
+      r.v[4 * q + 1] = x.y;
+      r.v[4 * q + 2] = x.z;
+      r.v[4 * q + 3] = x.w;
+    }
+#pragma unroll
+    for (int e = 0; e < DIR_ROWS; e++) {
+      if (i0 + e == 0 || r.v[e] != prev) r.f |= 1u << e;
+      prev = r.v[e];
+    }
+    return;
+  }
+  // the table's last rows
+#pragma unroll
+  for (int e = 0; e < DIR_ROWS; e++)
+    if (i0 + e < n) r.v[e] = rval[i0 + e];
 #pragma unroll
   for (int e = 0; e < DIR_ROWS; e++) {
     if (i0 + e < n && (i0 + e == 0 || r.v[e] != prev)) r.f |= 1u << e;
