@@ -684,11 +684,13 @@ def main() -> None:
     n_s = sum(j["S"].shape[0] for j in joins) / len(joins)
     n_r = sum(j["R"].shape[0] for j in joins) / len(joins)
     n_o = sum(j["n_out"] for j in joins) / len(joins)
-    names = ["build (R table: LSD radix passes + key directory)", "partition (S radix pass)",
-             "count (probe_count_kernel: every probe's run, stored as a descriptor; scan of the warp-tile totals)",
+    names = ["build (R table: two MSD radix passes, a shared-memory sort per bucket group, key directory)",
+             "partition (S radix pass)",
+             "count (probe_count_dir_kernel: every probe's directory entry, stored as its run descriptor; "
+             "scan of the warp-tile totals)",
              "write (probe_write_kernel: rows from the run descriptors at the scanned offsets)"]
-    kernel = ["rx_scatter_kernel+rx_hist_kernel (R)", "rx_scatter_kernel+rx_hist_kernel (S)",
-              "probe_count_kernel", "probe_write_kernel"]
+    kernel = ["msd_local_kernel+rx_scatter_kernel+rx_hist_kernel (R)", "rx_scatter_kernel+rx_hist_kernel (S)",
+              "probe_count_dir_kernel", "probe_write_kernel"]
     # algorithmic bytes per launch of each phase: the build reads R once and
     # writes its two columns (16 B per row), the partition reads and writes S
     # (16 B per tuple), the count reads the probe and writes its run
