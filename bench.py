@@ -4,10 +4,12 @@
 One step = the three hash joins of configuration C3 (R = 2^26 tuples holding
 2^24 distinct keys x4, S = 2^28 tuples with Zipf(s) keys over R's keys, 10% of
 S from an absent key range, s in {0, 0.75, 1}), each run end to end on the
-device: R table build (LSD radix passes + key directory), one S radix pass,
-one probe pass that finds, reserves and writes every result row.  Inputs are
-generated on the device with seeded integer generators (synthetic data;
-every input is far larger than the 126 MB L2).
+device as a caller sizing its output does: a count (R table build by two MSD
+radix passes, a shared-memory sort per bucket group and a key directory; one
+S radix pass; a count pass storing every probe's run descriptor), the count
+read back, an output of that size, then the write pass from the count's
+descriptors.  Inputs are generated on the device with seeded integer
+generators (synthetic data; every input is far larger than the 126 MB L2).
 
 Printed (rank 0, one JSON line):
   value      input tuples/s of the whole job (all ranks), inputs resident in HBM
