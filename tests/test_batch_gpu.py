@@ -57,3 +57,28 @@ def test_batch_duplicates_and_capacity(engine):
         engine.batch_hash_join(pairs, outs=views)
     assert ei.value.status == native.EJ_ERR_CAPACITY
     assert torch.all(outs[2][small:] == -9)
+
+
+def test_batch_with_large_joins(engine):
+    """Joins of 2^20 R rows and more in a batch (four segmented LSD passes
+    over every join's R, an in-place probe): mixed with small and medium ones
+    they give the same rows as alone, and a large one with too small an
+    output reports EJ_ERR_CAPACITY without writing past its end."""
+    sizes = [1 << 20, 700, 3000, (1 << 20) + 5, 40000, 1 << 21]
+    pairs = [request(engine, 100 + i, n, [1, 2, 8][i % 3]) for i, n in enumerate(sizes)]
+    got = engine.batch_hash_join(pairs)
+    for (R, S), rows in zip(pairs, got):
+        alone = engine.join("single_hash", R, S)
+        assert np.array_equal(O.canon(rows.cpu().numpy()), O.canon(alone.cpu().numpy()))
+    ref = O.hash_join(pairs[3][0].cpu().numpy(), pairs[3][1].cpu().numpy())
+    assert np.array_equal(O.canon(got[3].cpu().numpy()), O.canon(ref))
+    outs = [torch.full((max(r.shape[0], 1) + 64, 4), -9, dtype=torch.int32, device="cuda") for r in got]
+    views = [o[: max(r.shape[0], 1)] for o, r in zip(outs, got)]
+    small = got[0].shape[0] // 2
+    views[0] = outs[0][:small]
+    with pytest.raises(JoinError) as ei:
+        engine.batch_hash_join(pairs, outs=views)
+    assert ei.value.status == native.EJ_ERR_CAPACITY
+    assert torch.all(outs[0][small:] == -9)
+    for k in (1, 2, 3, 4, 5):  # the other joins are whole
+        assert np.array_equal(O.canon(views[k][: got[k].shape[0]].cpu().numpy()), O.canon(got[k].cpu().numpy()))
