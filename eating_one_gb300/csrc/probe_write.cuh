@@ -205,6 +205,25 @@ __device__ __forceinline__ void ej_emit_big_group(uint32_t c, unsigned long long
 __device__ __forceinline__ void ej_emit_warp(const EjProbeWarp& w, const int32_t (&kk)[PR_ITEMS][PW_PREFETCH],
                                              const ej_table_view& t, unsigned long long a,
                                              ej_result* __restrict__ out, uint64_t cap, int4* stage) {
+  // runs of at most one row throughout the tile (unique keys; an outer
+  // join's NULL-extended rows): each group's rows go straight out in lane
+  // order, positions from one ballot, no staging and no scans
+  bool one = true;
+#pragma unroll
+  for (int j = 0; j < PR_ITEMS; j++) one &= w.cnt[j] <= 1u;
+  if (__all_sync(EJ_FULL_MASK, one)) {
+    const unsigned int lt = ej_lanemask_lt();
+#pragma unroll
+    for (int j = 0; j < PR_ITEMS; j++) {
+      const unsigned int b = __ballot_sync(EJ_FULL_MASK, w.cnt[j] != 0u);
+      const unsigned long long p = a + (unsigned)__popc(b & lt);
+      if (w.cnt[j] && p < cap)
+        __stcs(reinterpret_cast<int4*>(out + p),
+               make_int4(kk[j][0], w.lo[j] == NULL_RUN ? EJ_NULL_KEY : w.s[j].y, w.s[j].x, w.s[j].y));
+      a += (unsigned)__popc(b);
+    }
+    return;
+  }
   uint32_t fill = 0;  // staged rows, the first of them at out[a]
 #pragma unroll
   for (int j = 0; j < PR_ITEMS; j++) {
