@@ -403,3 +403,41 @@ def test_bnl_unaligned_probe_side(engine):
     Sd = dev(np.concatenate([np.zeros((1, 2), np.int32), S]))[1:]
     assert Sd.data_ptr() % 16 == 8
     same_multiset(engine.join("bnl", dev(R), Sd), O.bnl_join(R, S))
+
+
+@pytest.mark.parametrize("case", ["dir_unaligned_probes", "dir_partial_tiles", "buckets_by_header"])
+def test_count_pass_over_a_packed_directory(engine, case):
+    """The count pass of a packed key directory takes two 128-probe tiles per
+    warp with 16-byte probe loads and stores each probe's directory entry as
+    its run descriptor; a probe side not 16-byte aligned, a last warp with
+    partial tiles, and a directory table whose build chose bucket bounds
+    (unique keys: the header's bits = 0) take its general path.  Count, then
+    the write from the count's descriptors, against the oracle."""
+    rng = np.random.default_rng({"dir_unaligned_probes": 61, "dir_partial_tiles": 62, "buckets_by_header": 63}[case])
+    if case == "buckets_by_header":
+        nR = 1 << 23  # the planner's class: a directory table; unique keys: bucket bounds
+        R = np.stack([np.arange(nR), rng.permutation(nR)], axis=1).astype(np.int32)
+        S = rel(rng, (1 << 20) + 77, 0, 2 * nR, key_base=nR)
+    else:
+        R = rel(rng, 60000, 0, 20000)  # runs of about three rows
+        S = rel(rng, 300077, 0, 30000, key_base=60000)  # 300077 = 1172 x 256 + 45
+    ref = O.hash_join(R, S)
+    Rd = dev(R)
+    if case == "dir_unaligned_probes":  # rows 8 bytes past a 16-byte boundary, probed in place
+        Sd = dev(np.vstack([np.zeros((1, 2), np.int32), S]))[1:]
+        assert Sd.data_ptr() % 16 == 8
+    else:
+        Sd = dev(S)
+    try:
+        if case != "buckets_by_header":
+            engine.set_option("table", native.EJ_TABLE_FORMAT_DIRECTORY)
+        if case == "dir_unaligned_probes":
+            engine.set_option("partition_bits", 0)
+        n = engine.count("hash", Rd, Sd)
+        assert n == len(ref)
+        out = torch.full((n + 16, 4), -7, dtype=torch.int32, device="cuda")
+        same_multiset(engine.hash_join(Rd, Sd, out=out[:n]), ref)
+        assert torch.all(out[n:] == -7)
+    finally:
+        engine.set_option("table", 0)
+        engine.set_option("partition_bits", -1)
