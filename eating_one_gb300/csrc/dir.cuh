@@ -162,15 +162,23 @@ __device__ __forceinline__ long long dir_tile_max(const int32_t* __restrict__ rv
   return all;
 }
 
+// slots of a tile's keys staged in shared memory, written out together
+constexpr int DIR_STAGE_SLOTS = 5120;  // 40 KB
+
 // the tile at row0 (first key rank k0, largest home_j - j of the keys before
 // it: kpre): every key's slots (pos_{k-1}, pos_k], holding {hash_k, start_k}
 // or, packed, {hash_k, start_k << 5 | min(run length, 31)}; the first and
-// last keys record their slots in the header
+// last keys record their slots in the header.  The tile's slots are one
+// range, (pos_{k0-1}, pos of its last key]: when it fits DIR_STAGE_SLOTS
+// (every tile but the first, whose leading slots dir_edges writes) the
+// entries are placed in shared memory and the range leaves in coalesced
+// stores, else each thread stores its keys' slots itself.
 __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval, uint64_t n, uint64_t row0,
                                                uint64_t k0, long long kpre, DirHeader* hdr, uint2* __restrict__ dir,
                                                bool packed) {
   __shared__ uint32_t tmp[DIR_THREADS / 32 + 1];
   __shared__ long long tmpl[DIR_THREADS / 32];
+  __shared__ uint2 stage[DIR_STAGE_SLOTS];
   const uint64_t i0 = row0 + threadIdx.x * DIR_ROWS;
   DirRows r;
   dir_rows(rval, n, i0, r);
@@ -189,6 +197,12 @@ __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval,
   long long all;
   long long run = max(kpre, dir_block_exclusive_max(m, tmpl, &all));  // max over keys before k
   long long prev = k ? (long long)k - 1 + run : -1;                   // pos_{k-1}
+  // the tile's range of slots: from one past pos_{k0-1} to the largest pos
+  // of its keys (a thread's last key: its rank plus its running maximum)
+  long long last;
+  dir_block_exclusive_max(r.f ? (long long)(k + __popc(r.f) - 1) + max(run, m) : LLONG_MIN, tmpl, &last);
+  const long long base = (long long)k0 + kpre;  // pos_{k0-1} + 1
+  const bool staged = k0 > 0 && total > 0 && last - base < (long long)DIR_STAGE_SLOTS;
   // a key's run ends at the thread's next key, else at the thread's last row
   // plus `tail`: the rows after the thread's that continue its last key
   // (counted up to a run of 31)
@@ -216,7 +230,10 @@ __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval,
     const uint32_t y = packed ? (uint32_t)(i0 + e) << 5 | min(len, 31u) : (uint32_t)(i0 + e);
     const uint2 entry = make_uint2(hv, y);
     // key 0's leading slots [0, pos_0) are written by dir_edges
-    for (long long g = (k ? prev + 1 : pos); g <= pos; g++) dir[g] = entry;
+    if (staged)
+      for (long long g = prev + 1; g <= pos; g++) stage[g - base] = entry;
+    else
+      for (long long g = (k ? prev + 1 : pos); g <= pos; g++) dir[g] = entry;
     if (k == 0) {
       hdr->pos_first = (unsigned long long)pos;
       hdr->lead = y;
@@ -224,6 +241,11 @@ __device__ __forceinline__ void dir_tile_place(const int32_t* __restrict__ rval,
     if (k + 1 == nk) hdr->pos_last = (unsigned long long)pos;
     prev = pos;
     k++;
+  }
+  if (staged) {
+    __syncthreads();
+    const uint32_t w = (uint32_t)(last - base + 1);
+    for (uint32_t i = threadIdx.x; i < w; i += DIR_THREADS) dir[base + i] = stage[i];
   }
 }
 
