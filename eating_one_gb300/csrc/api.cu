@@ -246,10 +246,10 @@ static const ej_tune_entry* tuning_for(const ej_handle* h, uint64_t nR) {
   return best;
 }
 
-int ej_tuned_bucket_delta(const ej_handle* h, uint64_t nR) {
+int ej_tuned_bucket_delta(const ej_handle* h, uint64_t nR, int planner) {
   if (h->opt_bucket_delta_set) return h->opt_bucket_delta;
   const ej_tune_entry* e = tuning_for(h, nR);
-  return e ? e->bucket_delta : 0;
+  return e ? e->bucket_delta : planner;
 }
 
 int ej_tuned_partition_bits(const ej_handle* h, uint64_t nR) {

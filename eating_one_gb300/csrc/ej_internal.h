@@ -242,7 +242,7 @@ struct ej_table_view {
 uint32_t ej_table_bucket_bits(uint64_t nR, int delta = 0);
 // the bucket-bits delta and the S partition bits (-1: planner) that apply to a
 // build side of nR rows: explicit options first, then the tuning table
-int ej_tuned_bucket_delta(const ej_handle* h, uint64_t nR);
+int ej_tuned_bucket_delta(const ej_handle* h, uint64_t nR, int planner = 0);
 int ej_tuned_partition_bits(const ej_handle* h, uint64_t nR);
 // the build's radix passes, the table format (0: planner) and the probe
 // kernels' warps per block that apply to a build side of nR rows
