@@ -161,7 +161,10 @@ __device__ __forceinline__ void batch_small_join(const BatchJoin& j, int4* smem,
 // large task waits behind them at the end.  (A resident grid pulling tasks
 // from an atomic counter measured slower: its loop needs 80 registers a
 // thread, three blocks per SM instead of four.)
-__global__ void __launch_bounds__(PR_THREADS)
+// (Four blocks per SM: 64 registers a thread; left free it takes 78, three
+// blocks, and the 256-instance batch ran 1% slower; at five blocks the
+// spills cost 20%.)
+__global__ void __launch_bounds__(PR_THREADS, 4)
 batch_task_kernel(const BatchJoin* __restrict__ joins, const BatchTask* __restrict__ tasks, ej_dev_status* st) {
   __shared__ int4 smem[PR_WARPS * PW_STAGE_ROWS];  // staging rows, or a small join's table
   static_assert(4 * BX_SMALL_R * sizeof(int32_t) <= sizeof(int4) * PR_WARPS * PW_STAGE_ROWS,
