@@ -622,8 +622,10 @@ uint32_t ej_probe_partition_bits(const ej_handle* h, uint64_t nR, uint64_t nS) {
   if (table <= l2 / 4.0) return 0;  // the whole table stays L2-resident
   // one partition's table region should be several MB so that the partitions
   // in flight share L2 with the streaming probe and output traffic (C3's
-  // 2^26-row tables: 7 bits; 5 to 8 bits measured within 2 % of each other)
-  uint32_t pb = ej_ceil_log2((uint64_t)(table / (l2 / 16.0)) + 1);
+  // 2^26-row tables: 6 bits, a region of L2/8 by the rows and buckets; with
+  // the key directory of a quarter load the count's region is 8 MB: the
+  // step 21.80 ms at 7 bits, 21.57 at 6)
+  uint32_t pb = ej_ceil_log2((uint64_t)(table / (l2 / 8.0)) + 1);
   if (pb > 8) pb = 8;
   if (pb > hb) pb = hb;
   return pb;
