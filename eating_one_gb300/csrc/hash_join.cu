@@ -198,12 +198,11 @@ probe_count_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_view t,
 // descriptor of the write pass (escape 31 included), so a probe costs its
 // hash, one 16-byte load of its home pair of slots (more only past smaller
 // hashes, or for a run of 31 rows or more) and the store of the entry's
-// second word.  Each warp takes
-// two 128-probe tiles, 8 probes per lane loaded two at a time (16-byte
-// loads), so that twice the directory loads are in flight per warp.  Tiles
-// that are not full (the last warp's) and tables whose build chose bucket
-// bounds (bits = 0 in the header) take the general path.  STORE: the
-// descriptors are kept for the write pass.
+// second word.  Each warp takes two 128-probe tiles, 8 probes per lane
+// loaded two at a time (16-byte loads), so that twice the directory loads
+// are in flight per warp.  Tiles that are not full (the last warp's) and
+// tables whose build chose bucket bounds (bits = 0 in the header) take the
+// general path.  STORE: the descriptors are kept for the write pass.
 constexpr int PCD_TILES = 2;  // warp tiles per warp
 
 template <bool STORE>
@@ -231,9 +230,10 @@ probe_count_dir_kernel(const ej_tuple* __restrict__ P, uint64_t nP, ej_table_vie
     }
     return;
   }
-  constexpr int N = 4 * PCD_TILES;  // probes per lane: 2 + 2j + {0, 1} of 64-probe half tile j
+  constexpr int N = 4 * PCD_TILES;  // probes per lane
   const uint32_t end = (uint32_t)t.nR << 5;  // entries at or past it: no key (sentinels)
-  // probe 2q + e of the lane sits at P[base + 64 q + 2 lane + e]
+  // probe 2q + e of the lane sits at P[base + 64 q + 2 lane + e]: probes
+  // 0..3 in the first tile, 4..7 in the second
   const int4* P4 = reinterpret_cast<const int4*>(P + base) + lane;
   uint32_t hv[N], slot[N];
   bool ok[N], hasb[N];
