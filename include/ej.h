@@ -124,7 +124,9 @@ typedef enum ej_option {
   EJ_OPT_PROBE_PARTITION_BITS = 0, /* radix bits of the one S partition pass, 0..8 (0 = probe
                                       in place); -1 (default) lets the planner choose */
   EJ_OPT_BUCKET_BITS_DELTA = 1,    /* hash-table buckets = 2^(ceil(log2|R|) - 2 + delta),
-                                      delta in -3..3, default 0 */
+                                      delta in -3..3; when neither this option nor the tuning
+                                      table sets it: 0 for single tables, 1 for the tables of
+                                      a batch */
   EJ_OPT_WAIT_LIMIT_NS = 2,        /* bound of every device-side wait of this handle's kernels
                                       (look-back scans, the nested loop's copy waits), in ns,
                                       0..10^10; -1 restores the default of 10^9 (1 s).  A wait
