@@ -405,16 +405,21 @@ def test_bnl_unaligned_probe_side(engine):
     same_multiset(engine.join("bnl", dev(R), Sd), O.bnl_join(R, S))
 
 
-@pytest.mark.parametrize("case", ["dir_unaligned_probes", "dir_partial_tiles", "buckets_by_header"])
+@pytest.mark.parametrize("case", ["dir_unaligned_probes", "dir_partial_tiles", "buckets_by_header", "dir_long_runs"])
 def test_count_pass_over_a_packed_directory(engine, case):
     """The count pass of a packed key directory takes two 128-probe tiles per
     warp with 16-byte probe loads and stores each probe's directory entry as
     its run descriptor; a probe side not 16-byte aligned, a last warp with
     partial tiles, and a directory table whose build chose bucket bounds
-    (unique keys: the header's bits = 0) take its general path.  Count, then
-    the write from the count's descriptors, against the oracle."""
-    rng = np.random.default_rng({"dir_unaligned_probes": 61, "dir_partial_tiles": 62, "buckets_by_header": 63}[case])
-    if case == "buckets_by_header":
+    (unique keys: the header's bits = 0) take its general path; a table of a
+    few long runs (40 keys) takes the escape of runs of 31 rows or more.
+    Count, then the write from the count's descriptors, against the oracle."""
+    rng = np.random.default_rng({"dir_unaligned_probes": 61, "dir_partial_tiles": 62, "buckets_by_header": 63,
+                                 "dir_long_runs": 64}[case])
+    if case == "dir_long_runs":  # 40 keys of about 1250 rows each
+        R = rel(rng, 50000, 0, 40)
+        S = rel(rng, 4000, -5, 45, key_base=50000)
+    elif case == "buckets_by_header":
         nR = 1 << 23  # the planner's class: a directory table; unique keys: bucket bounds
         R = np.stack([np.arange(nR), rng.permutation(nR)], axis=1).astype(np.int32)
         S = rel(rng, (1 << 20) + 77, 0, 2 * nR, key_base=nR)
